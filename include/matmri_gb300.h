@@ -1,0 +1,245 @@
+/*
+ * matmri_gb300.h — C ABI of the GB300 (sm_103a) MatMRI reconstruction hot path.
+ *
+ * Plain C: opaque handles, pointers and sizes; no C++ or torch types.
+ * Every entry point returns an int status (MMR_OK == 0); the message of the
+ * last failure on the calling thread is available from mmr_last_error().
+ *
+ * Data conventions (the MATLAB R2018a interleaved-complex API):
+ *   - complex data is interleaved complex64 (float re, float im);
+ *   - arrays are column-major with MATLAB index order: an image is
+ *     [imN(1), imN(2), ..., extra], samples are [M, extra];
+ *   - array pointers may be device pointers (gpuArray data) or host
+ *     pointers; host pointers are staged through device memory and the call
+ *     returns after the result is back on the host (nufftOp.m:335-347,396-398
+ *     accept host or gpuArray input the same way);
+ *   - trajectories, density compensation, coil maps and encoding phases are
+ *     given as host arrays at construction (the constructors of the
+ *     reference take MATLAB host arrays).
+ *   - `stream` is a cudaStream_t (NULL = the legacy default stream).
+ * Threading: a handle is used by one thread at a time; distinct handles are
+ * independent.
+ */
+#ifndef MATMRI_GB300_H
+#define MATMRI_GB300_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#if defined(__GNUC__)
+#define MMR_API __attribute__((visibility("default")))
+#else
+#define MMR_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MMR_OK              0
+#define MMR_ERR_BADARG      1   /* invalid argument / shape                      */
+#define MMR_ERR_NOMEM       2   /* device or host allocation failed              */
+#define MMR_ERR_CUDA        3   /* CUDA runtime error                            */
+#define MMR_ERR_TIMEOUT     4   /* a bounded device wait ran out                 */
+#define MMR_ERR_NONFINITE   5   /* NaN/Inf in an input where it is not allowed   */
+#define MMR_ERR_UNSUPPORTED 6   /* option combination not implemented            */
+
+#define MMR_ABI_VERSION 1
+
+typedef struct mmr_nufft mmr_nufft;   /* @nufftOp plan                 */
+typedef struct mmr_rcvr  mmr_rcvr;    /* @rcvrOp (precomputed maps)    */
+typedef struct mmr_sho   mmr_sho;     /* @sampHighOrder plan           */
+typedef struct mmr_sense mmr_sense;   /* mrSampFunc(., ., S, R, opt)   */
+
+/* ---- library ------------------------------------------------------------ */
+MMR_API int  mmr_abi_version(void);
+/* Copies the last error message of this thread (NUL-terminated). */
+MMR_API int  mmr_last_error(char* buf, size_t len);
+/* Device properties used by the autotuner (SM count, smem per block). */
+MMR_API int  mmr_device_info(int* sm_count, int* smem_optin_bytes, int* cc_major, int* cc_minor);
+
+/* ---- @nufftOp ------------------------------------------------------------
+ * Replaces nufftOp(imN, kloc, dcf, useGPU, os, kwidth)
+ *   (operators/@nufftOp/nufftOp.m:89-136; doPrep 138-274).
+ * kloc: host double [M x ndim] column-major, in [-0.5, 0.5) (values outside
+ *       wrap, as nufftOp.m:20-22 documents).  dcf: host double [M] or NULL.
+ * os <= 0 selects the reference default 1.5; kwidth <= 0 selects 6
+ *   (nufftOp.m:65-66). kwidth must be even, 2..8.                       */
+typedef struct mmr_nufft_desc {
+    int32_t       ndim;        /* 1, 2 or 3                                    */
+    int64_t       imN[3];
+    int64_t       nsamp;       /* M                                            */
+    const double* kloc;
+    const double* dcf;
+    double        os;
+    int32_t       kwidth;
+} mmr_nufft_desc;
+
+MMR_API int mmr_nufft_create(const mmr_nufft_desc* desc, mmr_nufft** out);
+/* Nop.dcf = dcf (demos/demo_regridding.m:35); dcf == NULL clears it. */
+MMR_API int mmr_nufft_set_dcf(mmr_nufft* plan, const double* dcf);
+/* osN, beta, Nkern of the plan (nufftOp.m:146-156). */
+MMR_API int mmr_nufft_info(const mmr_nufft* plan, int64_t osN[3], double* beta, int64_t* nkern);
+/* N*x (adjoint = 0: x [imN, nbatch] -> y [M, nbatch]) and N'*y (adjoint = 1)
+ * (nufftOp.m:284-408 incl. the extra-dim batching of 302-331).          */
+MMR_API int mmr_nufft_apply(mmr_nufft* plan, int adjoint, const void* in, void* out,
+                    int64_t nbatch, void* stream);
+/* prepToep: switches the plan to Toeplitz mode where apply() computes
+ * N'*(N*x) on a 2N grid (nufftOp.m:410-432, 348-352).  tos <= 0 selects
+ * 0.5*(os-1)+1, kwidth <= 0 the plan's kwidth.                         */
+MMR_API int mmr_nufft_prep_toep(mmr_nufft* plan, double tos, int32_t kwidth);
+MMR_API int mmr_nufft_destroy(mmr_nufft* plan);
+
+/* ---- @rcvrOp ---------------------------------------------------------------
+ * Replaces rcvrOp(maps, 0) (operators/@rcvrOp/rcvrOp.m:47-94, isCalDat = 0).
+ * maps: host complex64 [imN, C].                                         */
+MMR_API int mmr_rcvr_create(int32_t ndim, const int64_t imN[3], int64_t ncoil,
+                    const void* maps, mmr_rcvr** out);
+/* R*x (x [imN] -> [imN, C]) and R'*y (sum(y.*conj(maps), nDim+1))
+ * (rcvrOp.m:104-159).                                                    */
+MMR_API int mmr_rcvr_apply(mmr_rcvr* r, int adjoint, const void* in, void* out, void* stream);
+MMR_API int mmr_rcvr_destroy(mmr_rcvr* r);
+
+/* ---- @sampHighOrder --------------------------------------------------------
+ * Replaces sampHighOrder(b0, sampTimes, phs_spha, phs_conc, phs_grid, imMask)
+ *   (operators/@sampHighOrder/sampHighOrder.m:129-291, prepForDirect 496-588).
+ * Host doubles: b0 [V] rad/s (NULL = 0), t [M] s, spha [nspha x M],
+ * conc [nconc x M] (NULL when nconc = 0), grid x/y/z [V], mask [V] or NULL.
+ * nspha <= 36, nconc <= 4.                                                 */
+typedef struct mmr_sho_desc {
+    int32_t       ndim;        /* image dims (1..3)                           */
+    int64_t       imN[3];
+    int64_t       nsamp;       /* M = numel(sampTimes)                        */
+    int32_t       nspha;
+    int32_t       nconc;
+    const double* b0;
+    const double* t;
+    const double* spha;
+    const double* conc;
+    const double* gx;
+    const double* gy;
+    const double* gz;
+    const double* mask;
+} mmr_sho_desc;
+
+MMR_API int mmr_sho_create(const mmr_sho_desc* desc, mmr_sho** out);
+/* S*x (x [V, nbatch] -> y [M, nbatch]) and S'*y (useDirectWorker,
+ * sampHighOrder.m:361-391; the segmented approaches 2/3 compute the same
+ * sums, sampHighOrder.m:393-457).                                         */
+MMR_API int mmr_sho_apply(mmr_sho* s, int adjoint, const void* in, void* out,
+                  int64_t nbatch, void* stream);
+MMR_API int mmr_sho_destroy(mmr_sho* s);
+
+/* ---- mrSampFunc --------------------------------------------------------------
+ * Replaces opFunc = @(x,transp) mrSampFunc(x, transp, S, R, opt)
+ *   (operators/mrSampFunc.m:1-160) for S a nufftOp or sampHighOrder and R an
+ * rcvrOp (or none).  Exactly one of nufft / sho is non-NULL.
+ * W: host float [M] or [M x C] data weights (opt.W, mrSampFunc.m:126-128),
+ *    or NULL.  tikreg: opt.tikReg scalar (0 = none).                       */
+typedef struct mmr_sense_desc {
+    mmr_nufft*   nufft;
+    mmr_sho*     sho;
+    mmr_rcvr*    rcvr;
+    const float* W;
+    int32_t      w_per_coil;
+    double       tikreg;
+} mmr_sense_desc;
+
+MMR_API int mmr_sense_create(const mmr_sense_desc* desc, mmr_sense** out);
+/* transp = 0: image [imN] -> data [M, C];  transp = 1: data -> image.     */
+MMR_API int mmr_sense_apply(mmr_sense* a, int transp, const void* in, void* out, void* stream);
+/* A'*(A*x) with the fused gridding (used by cgne.m:215-218).             */
+MMR_API int mmr_sense_normal(mmr_sense* a, const void* in, void* out, void* stream);
+/* Tuning knobs chosen by the autotuner: coil chunk (0 = auto) and tile side. */
+MMR_API int mmr_sense_set_tuning(mmr_sense* a, int32_t coil_chunk, int32_t tile);
+MMR_API int mmr_sense_get_tuning(const mmr_sense* a, int32_t* coil_chunk, int32_t* tile);
+MMR_API int mmr_sense_destroy(mmr_sense* a);
+
+/* ---- cgne -------------------------------------------------------------------
+ * Replaces [x,resSqAll,mseAll,xnormAll,xdiffAll,stopThresh,status] =
+ *   cgne(A, b, x0, NitMax, opt, gam, R, W)  (iterativeSolvers/cgne.m:1-341).
+ * Options mirror cgne.m:21-89; a NaN double means MATLAB's [] (rule off).
+ * The whole iteration runs on the device (FP64 scalars and reductions,
+ * complex64 vectors) and is captured as a CUDA graph.                      */
+typedef struct mmr_cgne_opts {
+    int32_t       nit_max;           /* NitMax (<= 0 selects 1000)            */
+    double        res_thresh;        /* default 1e-10                         */
+    double        res_change_thresh; /* default []                            */
+    double        x_change_thresh;   /* default 1e-10                         */
+    int32_t       exp_res_n;         /* default 100                           */
+    double        nse_thresh_fact;   /* default 1.0                           */
+    int32_t       nse_extra_it;      /* default 4                             */
+    int32_t       stop_on_res_inc;   /* default 0                             */
+    double        res_inc_thresh;    /* default 1.0                           */
+    int32_t       stop_on_xdif_inc;  /* default 0                             */
+    double        noise_var;         /* default []                            */
+    const void*   noise;             /* optional noise draw [M x C] (complex64) for the
+                                        discrepancy rule; NULL = internal seeded draw */
+    uint64_t      noise_seed;
+    const void*   gtruth;            /* optional [imN] complex64 (opt.gtruth) */
+    const float*  tik_diag;          /* optional [imN] real: sum_k gam_k |R_k|^2 for
+                                        elementwise-mask R (cgne.m:171-179)  */
+    int32_t       w_per_coil;        /* W passed to mmr_cgne_solve is [M x C] */
+    int32_t       want_history;      /* 1: fill the history arrays            */
+} mmr_cgne_opts;
+
+/* Fills opts with cgne.m's defaults. */
+MMR_API int mmr_cgne_default_opts(mmr_cgne_opts* opts);
+
+/* History outputs (host doubles, capacity nit_max + nse_extra_it + 1 each;
+ * res_sq, mse, xnorm, xdiff are complex in the reference and are returned
+ * as their real parts). */
+typedef struct mmr_cgne_hist {
+    double* res_sq;
+    double* mse;
+    double* xnorm;
+    double* xdiff;
+    int32_t capacity;
+    int32_t n;            /* out: nit + 1 entries written                    */
+    double  stop_thresh;  /* out: NaN when no noise rule                     */
+    int32_t status;       /* out: cgne.m status code                         */
+    int32_t nit;          /* out                                              */
+} mmr_cgne_hist;
+
+/* b: data [M, C]; x0: image or NULL (x0 = A'*b, cgne.m:143-145);
+ * W: cgne's data weights [M] / [M x C] host float, or NULL. */
+MMR_API int mmr_cgne_solve(mmr_sense* A, const void* b, const void* x0, const float* W,
+                   const mmr_cgne_opts* opts, void* x_out, mmr_cgne_hist* hist,
+                   void* stream);
+
+/* ---- powermethod / bfista --------------------------------------------------
+ * powermethod(A, x0, NitMax, doAtA=1, xdiffThresh)  (iterativeSolvers/powermethod.m:1-67) */
+MMR_API int mmr_powermethod(mmr_sense* A, const void* x0, int32_t nit_max, double xdiff_thresh,
+                    double* max_eig_re, double* max_eig_im, void* stream);
+
+/* bfista(A, b, dwtND(J, imSize, false, 'db1'), lam, x0, NitMax, opt)
+ *   (iterativeSolvers/bfista.m:1-246; operators/@dwtND, undecimated Haar).
+ * levels[ndim]: J per dim; lam: per-band thresholds (nbands = 1 + sum over
+ * levels of (2^dims_decomposed - 1), band order low, high{1}{1..}, ...).
+ * max_eig <= 0: run powermethod (bfista.m:81-89).                          */
+typedef struct mmr_bfista_opts {
+    int32_t       nit_max;     /* default 200                                  */
+    double        res_thresh;  /* default 1e-5                                 */
+    double        max_eig;     /* opt.maxEig (<= 0 = [])                       */
+    int32_t       n_restart;   /* default NitMax + 1                           */
+    const void*   x_mask;      /* optional [imN] complex64                     */
+} mmr_bfista_opts;
+
+typedef struct mmr_bfista_hist {
+    double* res_sq;     /* capacity nit_max                                    */
+    double* rx;
+    double* test;       /* [nit_max x 2] column-major                          */
+    int32_t capacity;
+    int32_t n;          /* out: iterations run                                 */
+    double  max_eig;    /* out                                                 */
+} mmr_bfista_hist;
+
+MMR_API int mmr_bfista_solve(mmr_sense* A, const void* b, const int32_t* levels,
+                     const float* lam, int32_t nbands, const void* x0,
+                     const mmr_bfista_opts* opts, void* x_out, mmr_bfista_hist* hist,
+                     void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* MATMRI_GB300_H */

@@ -1,0 +1,183 @@
+"""rcvrOp, mrSampFunc and cgne on the GPU against the FP64 restatement
+(operators/@rcvrOp, operators/mrSampFunc.m, iterativeSolvers/cgne.m)."""
+import functools
+
+import numpy as np
+import pytest
+
+from gpu_util import crandn, rel
+from oracle.nufft_ref import NufftRef
+from oracle.sense_ref import RcvrRef, cgne_ref, mrsampfunc
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+
+
+@pytest.fixture(scope="module")
+def mm():
+    import matmri_gb300 as m
+    return m
+
+
+def _setup(mm, N=64, C=6, M=3000, dcf=False, seed=0, os_=2.0, kw=4):
+    from matmri_gb300 import synth
+    rng = np.random.default_rng(seed)
+    kloc = rng.uniform(-0.5, 0.5, (M, 2))
+    d = rng.uniform(0.2, 1, M) if dcf else None
+    maps = synth.coil_maps(N, C, seed)
+    S = mm.nufftOp([N, N], kloc, d, 1, os_, kw)
+    R = mm.rcvrOp(maps, 0)
+    Sr = NufftRef([N, N], kloc, d, os_, kw)
+    Rr = RcvrRef(maps)
+    return S, R, Sr, Rr, rng
+
+
+def test_rcvr(mm):
+    rng = np.random.default_rng(1)
+    maps = crandn(rng, (32, 32, 4))
+    R = mm.rcvrOp(maps, 0)
+    Rr = RcvrRef(maps)
+    x = crandn(rng, (32, 32))
+    y = crandn(rng, (32, 32, 4))
+    assert rel(R * x, Rr.mtimes(x)) < 1e-6
+    assert rel(R.H * y, Rr.H.mtimes(y)) < 1e-6
+
+
+@pytest.mark.parametrize("dcf", [False, True])
+@pytest.mark.parametrize("C", [1, 5, 8, 12])
+def test_mrsampfunc(mm, dcf, C):
+    S, R, Sr, Rr, rng = _setup(mm, C=C, dcf=dcf, seed=C)
+    x = crandn(rng, (64, 64))
+    y = crandn(rng, (3000, C))
+    op = mm.mrSampOp(S, R)
+    assert rel(op(x, "notransp"), mrsampfunc(x, "notransp", Sr, Rr)) < TOL
+    assert rel(op(y, "transp"), mrsampfunc(y, "transp", Sr, Rr)) < TOL
+    # the function-handle form
+    assert rel(mm.mrSampFunc(y, "transp", S, R), mrsampfunc(y, "transp", Sr, Rr)) < TOL
+    # fused normal operator == adjoint(forward)
+    ref_n = mrsampfunc(mrsampfunc(x, "notransp", Sr, Rr), "transp", Sr, Rr)
+    assert rel(op.normal(x), ref_n) < TOL
+
+
+@pytest.mark.parametrize("chunk", [1, 3, 8, 16])
+def test_coil_chunks(mm, chunk):
+    S, R, Sr, Rr, rng = _setup(mm, N=96, C=16, M=4000, seed=4)
+    op = mm.mrSampOp(S, R)
+    op.set_tuning(chunk, 0)
+    x = crandn(rng, (96, 96))
+    ref = mrsampfunc(mrsampfunc(x, "notransp", Sr, Rr), "transp", Sr, Rr)
+    assert rel(op.normal(x), ref) < TOL
+    y = crandn(rng, (4000, 16))
+    assert rel(op(y, "transp"), mrsampfunc(y, "transp", Sr, Rr)) < TOL
+
+
+def test_opt_W_and_vectorised(mm):
+    S, R, Sr, Rr, rng = _setup(mm, C=4, seed=7)
+    W = rng.uniform(0, 2, 3000)
+    opt = {"W": W, "imNFull": [64, 64], "daNFull": [3000, 4]}
+    op = mm.mrSampOp(S, R, opt)
+    y = crandn(rng, 3000 * 4)
+    assert rel(op(y, "transp"), mrsampfunc(y, "transp", Sr, Rr, opt)) < TOL
+    x = crandn(rng, 64 * 64)
+    assert rel(op(x, "notransp"), mrsampfunc(x, "notransp", Sr, Rr, opt)) < TOL
+
+
+def test_mrsampfunc_adjoint_identity(mm):
+    # mrSampFunc.m:163-215 adjoint dot-test incl. Tikhonov stacking
+    S, R, Sr, Rr, rng = _setup(mm, C=2, seed=11)
+    opt = {"imNFull": [64, 64], "daNFull": [3000, 2], "tikReg": 0.01}
+    A = mm.mrSampOp(S, R, opt)
+    x = crandn(rng, 64 * 64)
+    y = crandn(rng, 3000 * 2 + 64 * 64)
+    d1 = np.vdot(x, A(y, "transp"))
+    d2 = np.vdot(A(x, "notransp"), y)
+    assert abs(d1 - d2) / min(abs(d1), abs(d2)) < 1e-5
+
+
+def _cg_case(mm, seed=0, N=64, C=8, M=3000, dcf=False):
+    S, R, Sr, Rr, rng = _setup(mm, N=N, C=C, M=M, dcf=dcf, seed=seed)
+    from matmri_gb300 import synth
+    img = synth.ellipse_phantom(N, 10, seed, complex_phase=True)
+    data = mrsampfunc(img, "notransp", Sr, Rr)
+    data = synth.add_noise(data, 30.0, seed + 1)
+    A = mm.mrSampOp(S, R)
+    Aref = lambda x, t: mrsampfunc(x, t, Sr, Rr)
+    return A, Aref, data, img
+
+
+def test_cgne_fixed_iterations(mm):
+    A, Aref, data, img = _cg_case(mm, seed=3)
+    opt = {"xChangeThresh": None, "resThresh": None}
+    x, rs, mse, xn, xd, st, status = mm.cgne(A, data, None, 12, opt)
+    xr, rsr, _, xnr, xdr, str_, statr = cgne_ref(Aref, data, None, 12, opt)
+    assert status == statr == 0 and len(rs) == len(rsr) == 13
+    assert rel(x, xr) < 1e-4
+    assert np.allclose(rs, rsr.real, rtol=1e-3)
+    assert np.allclose(xn, xnr.real, rtol=1e-4)
+    assert np.allclose(xd[1:], xdr[1:].real, rtol=1e-2)
+
+
+def test_cgne_with_W_x0_and_gtruth(mm):
+    A, Aref, data, img = _cg_case(mm, seed=5, C=4)
+    rng = np.random.default_rng(2)
+    W = rng.uniform(0.5, 1.5, 3000)
+    x0 = np.zeros((64, 64), complex)
+    opt = {"xChangeThresh": None, "resThresh": None, "gtruth": img, "expResN": 4}
+    x, rs, mse, *_ = mm.cgne(A, data, x0, 10, opt, None, None, W)
+    xr, rsr, mser, *_ = cgne_ref(Aref, data, x0, 10, opt, None, None, W)
+    assert rel(x, xr) < 1e-4
+    assert np.allclose(mse, mser.real, rtol=1e-3)
+
+
+def test_cgne_tikhonov_mask(mm):
+    A, Aref, data, img = _cg_case(mm, seed=6, C=4)
+    mask = np.random.default_rng(4).uniform(0, 1, (64, 64))
+    opt = {"xChangeThresh": None, "resThresh": None}
+    x, *_ = mm.cgne(A, data, None, 8, opt, 0.5, mask)
+    xr, *_ = cgne_ref(Aref, data, None, 8, opt, 0.5, mask)
+    assert rel(x, xr) < 1e-4
+
+
+@pytest.mark.parametrize("rule", ["resChange", "resInc", "xdifInc", "xChange", "noise"])
+def test_cgne_stopping_rules(mm, rule):
+    A, Aref, data, img = _cg_case(mm, seed=8, C=4)
+    opt = {"xChangeThresh": None, "resThresh": None}
+    if rule == "resChange":
+        opt["resChangeThresh"] = 0.05
+    elif rule == "resInc":
+        opt.update(stopOnResInc=1, resIncThresh=0.5)
+    elif rule == "xdifInc":
+        opt.update(stopOnXdifInc=1)
+    elif rule == "xChange":
+        xr0, rsr0, _, _, xdr0, *_ = cgne_ref(Aref, data, None, 6, dict(opt))
+        opt["xChangeThresh"] = float(xdr0[4].real) * 1.01
+    elif rule == "noise":
+        noise = 0.05 * (np.random.default_rng(1).standard_normal(data.shape)
+                        + 1j * np.random.default_rng(2).standard_normal(data.shape))
+        opt.update(noiseVar=1.0, noise=noise.astype(np.complex64), nseThreshFact=200.0)
+    x, rs, _, _, xd, st, status = mm.cgne(A, data, None, 30, opt)
+    xr, rsr, _, _, xdr, str_, statr = cgne_ref(Aref, data, None, 30, opt,
+                                               noise=opt.get("noise").astype(np.complex128) if rule == "noise" else None)
+    assert status == statr, (rule, status, statr)
+    assert len(rs) == len(rsr), (rule, len(rs), len(rsr))
+    assert rel(x, xr) < 1e-4
+    if rule == "noise":
+        assert abs(st - str_) / str_ < 1e-4
+
+
+def test_cgne_partial_handle_and_torch(mm):
+    torch = pytest.importorskip("torch")
+    S, R, Sr, Rr, rng = _setup(mm, C=4, seed=9)
+    A = functools.partial(mm.mrSampFunc, samplingOp=S, R=R)
+    data = crandn(rng, (3000, 4)).astype(np.complex64)
+    opt = {"xChangeThresh": None, "resThresh": None}
+    x1, *_ = mm.cgne(A, data, None, 5, opt)
+    x2, *_ = mm.cgne(A, torch.from_numpy(data).cuda(), None, 5, opt)
+    assert x2.is_cuda
+    assert rel(x2.cpu().numpy(), x1) < 1e-5
+
+
+def test_cgne_rejects_python_callable(mm):
+    S, R, *_ = _setup(mm, C=2, seed=1)
+    with pytest.raises(TypeError):
+        mm.cgne(lambda x, t: x, np.zeros((3000, 2), complex), None, 3)

@@ -1,0 +1,85 @@
+"""sampHighOrder on the GPU against the FP64 restatement and the reference's
+known-answer tests (operators/@sampHighOrder/tests.m)."""
+import numpy as np
+import pytest
+
+from gpu_util import crandn, rel
+from oracle.nufft_ref import fftnc
+from oracle.sho_ref import ShoRef
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def mm():
+    import matmri_gb300 as m
+    return m
+
+
+def _rand_case(rng, imN, kN):
+    b0 = rng.standard_normal(imN) + rng.uniform()
+    t = rng.standard_normal(kN) / np.sqrt(np.prod(kN))
+    spha = rng.standard_normal([16] + list(kN))
+    conc = rng.standard_normal([4] + list(kN))
+    grid = {k: rng.standard_normal(imN) for k in "xyz"}
+    return b0, t, spha, conc, grid
+
+
+@pytest.mark.parametrize("nd", [1, 2, 3])
+def test_random_vs_oracle_and_adjoint(mm, nd):
+    # @sampHighOrder/tests.m:10-28 shapes (N0 = 64)
+    rng = np.random.default_rng(nd)
+    N0 = 64
+    imN = [round(N0 ** (2 / nd))] * nd
+    kN = [round(N0 ** (1 / nd))] * nd
+    b0, t, spha, conc, grid = _rand_case(rng, imN, kN)
+    S = mm.sampHighOrder(b0, t, spha, conc, grid, None, 1, 0, 0)
+    Sr = ShoRef(b0, t, spha, conc, grid)
+    x = crandn(rng, imN + [2])
+    y = crandn(rng, kN + [2])
+    assert rel(S * x, Sr.mtimes(x)) < 1e-5
+    assert rel(S.H * y, Sr.H.mtimes(y)) < 1e-5
+    d1 = np.vdot(x.reshape(-1, order="F"), (S.H * y).reshape(-1, order="F"))
+    d2 = np.vdot((S * x).reshape(-1, order="F"), y.reshape(-1, order="F"))
+    assert abs(d1 - d2) / min(abs(d1), abs(d2)) < 1e-5
+
+
+def test_segmented_approaches_equal(mm):
+    # @sampHighOrder/tests.m:30-41: approaches 2 and 3 equal the direct one
+    rng = np.random.default_rng(4)
+    b0, t, spha, conc, grid = _rand_case(rng, [16, 16], [64])
+    x = crandn(rng, (16, 16, 2))
+    ys = [mm.sampHighOrder(b0, t, spha, conc, grid, None, 1, 0, a, {"segmentedNdiv": 2}) * x for a in (0, 2, 3)]
+    assert rel(ys[1], ys[0]) < 1e-6 and rel(ys[2], ys[0]) < 1e-6
+
+
+def test_fourier_equivalence(mm):
+    # @sampHighOrder/tests.m:265-283 (phase = Cartesian linear ramp -> centered FFT)
+    N = 64
+    gx, gy = np.meshgrid(np.arange(-N / 2, N / 2), np.arange(-N / 2, N / 2))
+    grid = {"x": gx.astype(float), "y": gy.astype(float), "z": np.zeros((N, N))}
+    spha = np.zeros((16, N, N))
+    conc = np.zeros((4, N, N))
+    spha[2] = np.pi * 2 / N * np.tile(np.arange(-N / 2, N / 2), N).reshape(N, N, order="F")
+    spha[1] = np.pi * 2 / N * np.tile(np.arange(-N / 2, N / 2), (N, 1))
+    t = np.arange(N * N, dtype=float).reshape(N, N, order="F")
+    im0 = np.random.default_rng(0).uniform(0, 1, (N, N))
+    S = mm.sampHighOrder(np.zeros((N, N)), t, spha, conc, grid, None, 1, 0, 0)
+    k0 = np.reshape(S * im0, (N, N), order="F")
+    k1 = fftnc(im0, 2)
+    cost = np.sqrt(np.sum((np.abs(k0) - np.abs(k1)) ** 2)) / k0.size
+    assert cost < 1e-6
+    im1 = np.reshape(S.H * k0, (N, N), order="F")
+    assert np.sqrt(np.sum(np.abs(im1 - im0) ** 2)) / im0.size < 1e-6
+
+
+def test_highorder_workload_small(mm):
+    from matmri_gb300 import synth
+    b0, t, spha, conc, grid = synth.highorder_inputs(N=32, M=2048, seed=5)
+    S = mm.sampHighOrder(b0, t, spha, conc, grid)
+    Sr = ShoRef(b0, t, spha, conc, grid)
+    rng = np.random.default_rng(1)
+    x = crandn(rng, (32, 32, 4))
+    y = crandn(rng, (2048, 4))
+    assert rel(S * x, Sr.mtimes(x)) < 1e-5
+    assert rel(S.H * y, Sr.H.mtimes(y)) < 1e-5

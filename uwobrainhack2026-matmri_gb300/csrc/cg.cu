@@ -1,0 +1,523 @@
+// cgne (iterativeSolvers/cgne.m) as a device-resident solver.
+//
+// Vectors (x, p, res, Ap) are complex64; every inner product, alph, beta and
+// the stopping tests are FP64.  One iteration is captured as a CUDA graph:
+//   Ap = A'(W.*A(p)) [+ gam R'R p]          (cgne.m:214-227)
+//   alph = res_sq_old / (p' Ap)             (228)
+//   x = xold + alph p                       (229)
+//   res = b - A'(W.*A(x)) ... (explicit, mod(nit, expResN) == 0, beta = 0)  (230-246)
+//   res = res - alph Ap       (otherwise)   (248)
+//   histories, stopping rules               (252-326)
+//   p = res + beta p                        (328)
+// The last block of each reduction kernel runs the scalar epilogue, so the
+// host never synchronises inside the loop; a device flag stops all later
+// kernels once a rule fires, and the host polls it between graph batches only
+// when a data-dependent rule is enabled.
+#include <algorithm>
+#include <cmath>
+#include <random>
+
+#include "sense.cuh"
+
+namespace mmr {
+
+struct CgState {
+    double res_sq_old;
+    double pAp_re, pAp_im;
+    double acc_res, acc_xn, acc_xd, acc_mse;
+    double beta;
+    double stop_thresh;
+    // options
+    double resThresh, resChangeThresh, xChangeThresh, resIncThresh;
+    int has_resThresh, has_resChange, has_xChange, has_stop;
+    int stopOnResInc, stopOnXdifInc, nseExtraIt;
+    int findxnorm, findxdiff, has_gt;
+    int cap;
+    // progress
+    int nit, nitmax, finished, status;
+    int resIncs, xdifIncs, lastXdifInc;
+    unsigned int counter;
+};
+
+struct CgWorkspace {
+    long long n = 0;
+    DevBuf x, p, res, Ap, b, tmp, tik, gt, state, hist, noise, nimg;
+    Staged sb, sxo;
+    // graph cache
+    cudaGraphExec_t g_norm = nullptr, g_expl = nullptr;
+    const void* key[8] = {nullptr};
+    long long keyv[4] = {0};
+    ~CgWorkspace() {
+        if (g_norm) cudaGraphExecDestroy(g_norm);
+        if (g_expl) cudaGraphExecDestroy(g_expl);
+    }
+};
+
+void cg_release(SenseOp& a) {
+    delete static_cast<CgWorkspace*>(a.solver_ws);
+    a.solver_ws = nullptr;
+}
+
+// ------------------------------------------------------------- reductions ----
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o >= 1; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// Block-reduces up to 4 doubles; thread 0 atomically adds them to dst[0..n-1].
+template <int NV>
+__device__ __forceinline__ void block_accumulate(double (&v)[NV], double* const (&dst)[NV]) {
+    __shared__ double red[NV][32];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        const double s = warp_sum(v[k]);
+        if (lane == 0) red[k][warp] = s;
+    }
+    __syncthreads();
+    if (warp == 0) {
+        const int nw = blockDim.x >> 5;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            double s = lane < nw ? red[k][lane] : 0.0;
+            s = warp_sum(s);
+            if (lane == 0 && dst[k]) atomicAdd(dst[k], s);
+        }
+    }
+}
+
+// True in exactly one thread (thread 0 of the last block to arrive).
+__device__ __forceinline__ bool last_block(CgState* st) {
+    __shared__ bool last;
+    __threadfence();
+    __syncthreads();
+    if (threadIdx.x == 0) last = atomicAdd(&st->counter, 1u) == gridDim.x - 1;
+    __syncthreads();
+    if (last && threadIdx.x == 0) {
+        __threadfence();
+        return true;
+    }
+    return false;
+}
+
+// Scalar epilogue of one iteration (cgne.m:252-335).
+__device__ void cg_finalize(CgState* st, double* hist, bool expl) {
+    volatile CgState* vs = st;
+    const int nit = vs->nit;
+    const int cap = vs->cap;
+    double* hr = hist;
+    double* hm = hist + cap;
+    double* hxn = hist + 2 * cap;
+    double* hxd = hist + 3 * cap;
+    const double rsn = vs->acc_res;
+    const int k = nit + 1;
+    if (k < cap) {
+        hr[k] = rsn;
+        if (vs->findxnorm) hxn[k] = vs->acc_xn;
+        if (vs->findxdiff) hxd[k] = vs->acc_xd;
+        if (vs->has_gt) hm[k] = vs->acc_mse;
+    }
+    int finished = 0, status = vs->status;
+    const double xd = vs->findxdiff ? vs->acc_xd : 0.0;
+    if (vs->has_xChange && xd < vs->xChangeThresh) { finished = 1; status = 10; }
+    if (vs->has_resThresh && rsn < vs->resThresh) { finished = 1; status = 1; }
+    if (vs->has_resChange && fabs((rsn - hr[nit]) / hr[nit]) < vs->resChangeThresh) { finished = 1; status = 2; }
+    int nitmax = vs->nitmax;
+    if (vs->has_stop && rsn < vs->stop_thresh) {
+        nitmax = nit + vs->nseExtraIt;
+        vs->stop_thresh = 0.0;
+        status = 3;
+    }
+    if (vs->stopOnResInc > 0 && rsn / hr[nit] > vs->resIncThresh) {
+        vs->resIncs = vs->resIncs + 1;
+        if (vs->resIncs >= vs->stopOnResInc) { finished = 1; status = 4; }
+    }
+    const double xdprev = vs->findxdiff ? hxd[nit] : 0.0;
+    if (vs->stopOnXdifInc > 0 && xd > xdprev) {
+        if (!vs->lastXdifInc) {
+            vs->xdifIncs = vs->xdifIncs + 1;
+            vs->lastXdifInc = 1;
+            if (vs->xdifIncs >= vs->stopOnXdifInc) { finished = 1; status = 5; }
+        }
+    } else {
+        vs->lastXdifInc = 0;
+    }
+    vs->beta = expl ? 0.0 : rsn / vs->res_sq_old;
+    vs->res_sq_old = rsn;
+    const int nn = nit + 1;
+    if (nn >= nitmax) { finished = 1; status = 0; }
+    vs->nit = nn;
+    vs->nitmax = nitmax;
+    vs->status = status;
+    vs->pAp_re = vs->pAp_im = 0.0;
+    vs->acc_res = vs->acc_xn = vs->acc_xd = vs->acc_mse = 0.0;
+    vs->counter = 0;
+    __threadfence();
+    if (finished) vs->finished = 1;
+}
+
+// res = b - Ax - tik.*x0 ; p = res ; histories at index 0 (cgne.m:164-207)
+__global__ void cg_init_kernel(const float2* __restrict__ b, const float2* __restrict__ ax,
+                               const float2* __restrict__ x, const float* __restrict__ tik,
+                               const float2* __restrict__ gt, float2* __restrict__ res, float2* __restrict__ p,
+                               long long n, CgState* st, double* hist) {
+    double v[4] = {0, 0, 0, 0};
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float2 xi = x[i];
+        float2 r = csub(b[i], ax[i]);
+        if (tik) r = make_float2(r.x - tik[i] * xi.x, r.y - tik[i] * xi.y);
+        res[i] = r;
+        p[i] = r;
+        v[0] += (double)r.x * r.x + (double)r.y * r.y;
+        v[1] += (double)xi.x * xi.x + (double)xi.y * xi.y;
+        if (gt) {
+            const double dx = (double)gt[i].x - xi.x, dy = (double)gt[i].y - xi.y;
+            v[2] += dx * dx + dy * dy;
+        }
+    }
+    double* const dst[4] = {&st->acc_res, &st->acc_xn, &st->acc_mse, nullptr};
+    block_accumulate<4>(v, dst);
+    if (last_block(st)) {
+        volatile CgState* vs = st;
+        const int cap = vs->cap;
+        const double r0 = vs->acc_res;
+        hist[0] = r0;
+        const double xn = vs->findxnorm ? vs->acc_xn : 0.0;
+        hist[2 * cap] = xn;
+        hist[3 * cap] = vs->findxdiff ? xn : 0.0;
+        hist[cap] = vs->has_gt ? vs->acc_mse : 0.0;
+        vs->res_sq_old = r0;
+        vs->pAp_re = vs->pAp_im = 0.0;
+        vs->acc_res = vs->acc_xn = vs->acc_xd = vs->acc_mse = 0.0;
+        vs->counter = 0;
+    }
+}
+
+// Ap += tik.*p ; pAp = p' * Ap
+__global__ void cg_pap_kernel(const float2* __restrict__ p, float2* __restrict__ Ap, const float* __restrict__ tik,
+                              long long n, CgState* st) {
+    if (st->finished) return;
+    double v[2] = {0, 0};
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float2 pi = p[i];
+        float2 a = Ap[i];
+        if (tik) {
+            a = make_float2(a.x + tik[i] * pi.x, a.y + tik[i] * pi.y);
+            Ap[i] = a;
+        }
+        v[0] += (double)pi.x * a.x + (double)pi.y * a.y;    // re(conj(p) a)
+        v[1] += (double)pi.x * a.y - (double)pi.y * a.x;    // im(conj(p) a)
+    }
+    double* const dst[2] = {&st->pAp_re, &st->pAp_im};
+    block_accumulate<2>(v, dst);
+}
+
+// mode 0: x += alph p, res -= alph Ap, all accumulators, finalize.
+// mode 1: x += alph p only (explicit-residual iteration); finalize happens later.
+template <int MODE>
+__global__ void cg_update_kernel(float2* __restrict__ x, const float2* __restrict__ p, const float2* __restrict__ Ap,
+                                 float2* __restrict__ res, const float2* __restrict__ gt, long long n, CgState* st,
+                                 double* hist) {
+    if (st->finished) return;
+    const double rso = st->res_sq_old, ar = st->pAp_re, ai = st->pAp_im;
+    const double den = ar * ar + ai * ai;
+    const double alr = rso * ar / den, ali = -rso * ai / den;     // res_sq_old / (p' Ap)
+    double v[4] = {0, 0, 0, 0};
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float2 pi = p[i];
+        const float2 xo = x[i];
+        const float2 xn = make_float2((float)((double)xo.x + alr * pi.x - ali * pi.y),
+                                      (float)((double)xo.y + alr * pi.y + ali * pi.x));
+        x[i] = xn;
+        const double dx = (double)xn.x - xo.x, dy = (double)xn.y - xo.y;
+        v[1] += (double)xn.x * xn.x + (double)xn.y * xn.y;
+        v[2] += dx * dx + dy * dy;
+        if (gt) {
+            const double ex = (double)gt[i].x - xn.x, ey = (double)gt[i].y - xn.y;
+            v[3] += ex * ex + ey * ey;
+        }
+        if (MODE == 0) {
+            const float2 a = Ap[i], r = res[i];
+            const float2 rn = make_float2((float)((double)r.x - (alr * a.x - ali * a.y)),
+                                          (float)((double)r.y - (alr * a.y + ali * a.x)));
+            res[i] = rn;
+            v[0] += (double)rn.x * rn.x + (double)rn.y * rn.y;
+        }
+    }
+    double* const dst[4] = {MODE == 0 ? &st->acc_res : nullptr, &st->acc_xn, &st->acc_xd, &st->acc_mse};
+    block_accumulate<4>(v, dst);
+    if (MODE == 0) {
+        if (last_block(st)) cg_finalize(st, hist, false);
+    } else {
+        // keep the block counter consistent: mode 1 does not finalize
+    }
+}
+
+// Explicit residual: res = b - Ax - tik.*x ; finalize with beta = 0.
+__global__ void cg_res_explicit_kernel(const float2* __restrict__ b, const float2* __restrict__ ax,
+                                       const float2* __restrict__ x, const float* __restrict__ tik,
+                                       float2* __restrict__ res, long long n, CgState* st, double* hist) {
+    if (st->finished) return;
+    double v[1] = {0};
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        float2 r = csub(b[i], ax[i]);
+        if (tik) r = make_float2(r.x - tik[i] * x[i].x, r.y - tik[i] * x[i].y);
+        res[i] = r;
+        v[0] += (double)r.x * r.x + (double)r.y * r.y;
+    }
+    double* const dst[1] = {&st->acc_res};
+    block_accumulate<1>(v, dst);
+    if (last_block(st)) cg_finalize(st, hist, true);
+}
+
+__global__ void cg_p_kernel(float2* __restrict__ p, const float2* __restrict__ res, long long n, const CgState* st) {
+    // runs after the finalize of the same iteration: skip only if finished *before* it
+    const double beta = st->beta;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float2 r = res[i], pi = p[i];
+        p[i] = make_float2((float)((double)r.x + beta * pi.x), (float)((double)r.y + beta * pi.y));
+    }
+}
+
+__global__ void norm2_kernel(const float2* __restrict__ v, long long n, double* out) {
+    double s[1] = {0};
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        s[0] += (double)v[i].x * v[i].x + (double)v[i].y * v[i].y;
+    double* const dst[1] = {out};
+    block_accumulate<1>(s, dst);
+}
+
+static unsigned red_grid(long long n) {
+    const long long b = cdiv(n, 256);
+    return (unsigned)std::max<long long>(1, std::min<long long>(b, 2LL * device_sm_count()));
+}
+
+static bool isset(double v) { return !std::isnan(v); }
+
+// Captures one iteration (explicit or not) on `st`.
+static cudaGraphExec_t capture_iter(SenseOp& a, CgWorkspace& w, bool expl, bool has_tik, bool has_gt) {
+    cudaStream_t st = a.stream;
+    CgState* sp = w.state.as<CgState>();
+    double* hist = w.hist.as<double>();
+    const long long n = w.n;
+    const int* active = &sp->finished;
+    const unsigned g = red_grid(n);
+    float2* x = w.x.as<float2>();
+    float2* p = w.p.as<float2>();
+    float2* res = w.res.as<float2>();
+    float2* Ap = w.Ap.as<float2>();
+    const float* tik = has_tik ? w.tik.as<float>() : nullptr;
+    const float2* gt = has_gt ? w.gt.as<float2>() : nullptr;
+    MMR_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+    try {
+        sense_normal(a, p, Ap, st, active);
+        cg_pap_kernel<<<g, 256, 0, st>>>(p, Ap, tik, n, sp);
+        if (expl) {
+            cg_update_kernel<1><<<g, 256, 0, st>>>(x, p, Ap, res, gt, n, sp, hist);
+            sense_normal(a, x, w.tmp.as<float2>(), st, active);
+            cg_res_explicit_kernel<<<g, 256, 0, st>>>(w.b.as<float2>(), w.tmp.as<float2>(), x, tik, res, n, sp, hist);
+        } else {
+            cg_update_kernel<0><<<g, 256, 0, st>>>(x, p, Ap, res, gt, n, sp, hist);
+        }
+        cg_p_kernel<<<g, 256, 0, st>>>(p, res, n, sp);
+    } catch (...) {
+        cudaGraph_t gr;
+        cudaStreamEndCapture(st, &gr);
+        if (gr) cudaGraphDestroy(gr);
+        throw;
+    }
+    cudaGraph_t gr = nullptr;
+    MMR_CUDA(cudaStreamEndCapture(st, &gr));
+    cudaGraphExec_t ex = nullptr;
+    cudaError_t e = cudaGraphInstantiate(&ex, gr, 0);
+    cudaGraphDestroy(gr);
+    MMR_CUDA(e);
+    return ex;
+}
+
+static void cg_solve(SenseOp& a, const void* b_user, const void* x0_user, const float* W, const mmr_cgne_opts& o,
+                     void* x_user, mmr_cgne_hist* hist, cudaStream_t ust) {
+    if (!a.solver_ws) a.solver_ws = new CgWorkspace();
+    CgWorkspace& w = *static_cast<CgWorkspace*>(a.solver_ws);
+    const long long n = a.Nimg;
+    const long long nd = a.M * a.C;
+    w.n = n;
+    for (DevBuf* bb : {&w.x, &w.p, &w.res, &w.Ap, &w.b, &w.tmp}) bb->ensure(n * sizeof(float2));
+    const int nitmax0 = o.nit_max > 0 ? o.nit_max : 1000;
+    const int extra = std::max(0, o.nse_extra_it);
+    const int cap = nitmax0 + extra + 1;
+    w.state.ensure(sizeof(CgState));
+    w.hist.ensure((size_t)4 * cap * sizeof(double));
+    cudaStream_t st = a.stream;
+    // order the internal stream after the caller's stream
+    cudaEvent_t ev;
+    MMR_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    MMR_CUDA(cudaEventRecord(ev, ust));
+    MMR_CUDA(cudaStreamWaitEvent(st, ev, 0));
+
+    sense_set_weights(a, W, W && o.w_per_coil);
+    // inputs
+    const float2* b_in = (const float2*)stage_in(w.sb, b_user, (size_t)nd * 8, st);
+    const bool has_tik = o.tik_diag != nullptr;
+    const bool has_gt = o.gtruth != nullptr;
+    if (has_tik) {
+        w.tik.ensure(n * sizeof(float));
+        MMR_CUDA(cudaMemcpyAsync(w.tik.p, o.tik_diag, n * sizeof(float), cudaMemcpyDefault, st));
+    }
+    if (has_gt) {
+        w.gt.ensure(n * sizeof(float2));
+        MMR_CUDA(cudaMemcpyAsync(w.gt.p, o.gtruth, n * sizeof(float2), cudaMemcpyDefault, st));
+    }
+    // b = A'(W.*bin)  (cgne.m:136-140)
+    sense_adjoint(a, b_in, w.b.as<float2>(), st, nullptr);
+    if (x0_user) MMR_CUDA(cudaMemcpyAsync(w.x.p, x0_user, n * 8, cudaMemcpyDefault, st));
+    else MMR_CUDA(cudaMemcpyAsync(w.x.p, w.b.p, n * 8, cudaMemcpyDeviceToDevice, st));   // x0 = b (143-145)
+
+    CgState h = {};
+    h.resThresh = o.res_thresh;
+    h.has_resThresh = isset(o.res_thresh);
+    h.resChangeThresh = o.res_change_thresh;
+    h.has_resChange = isset(o.res_change_thresh);
+    h.xChangeThresh = o.x_change_thresh;
+    h.has_xChange = isset(o.x_change_thresh);
+    h.resIncThresh = o.res_inc_thresh;
+    h.stopOnResInc = o.stop_on_res_inc;
+    h.stopOnXdifInc = o.stop_on_xdif_inc;
+    h.nseExtraIt = o.nse_extra_it;
+    h.findxnorm = 1;                                   // nargout > 3 (histories requested)
+    h.findxdiff = 1;
+    h.has_gt = has_gt;
+    h.cap = cap;
+    h.nitmax = nitmax0;
+    h.stop_thresh = 0;
+    h.has_stop = 0;
+    // discrepancy-principle threshold (148-162)
+    if (isset(o.noise_var) && o.noise_var > 0) {
+        w.noise.ensure((size_t)nd * 8);
+        if (o.noise) {
+            MMR_CUDA(cudaMemcpyAsync(w.noise.p, o.noise, (size_t)nd * 8, cudaMemcpyDefault, st));
+        } else {
+            std::mt19937_64 gen(o.noise_seed);
+            std::normal_distribution<double> nrm(0.0, 1.0);
+            std::vector<float2> nz(nd);
+            const double s = std::sqrt(o.noise_var / 2.0);
+            for (auto& z : nz) z = make_float2((float)(s * nrm(gen)), (float)(s * nrm(gen)));
+            MMR_CUDA(cudaMemcpyAsync(w.noise.p, nz.data(), (size_t)nd * 8, cudaMemcpyHostToDevice, st));
+            MMR_CUDA(cudaStreamSynchronize(st));
+        }
+        w.nimg.ensure(n * 8 + 64);
+        sense_adjoint(a, w.noise.as<float2>(), w.nimg.as<float2>(), st, nullptr);
+        double* acc = reinterpret_cast<double*>(w.nimg.as<char>() + n * 8);
+        MMR_CUDA(cudaMemsetAsync(acc, 0, sizeof(double), st));
+        norm2_kernel<<<red_grid(n), 256, 0, st>>>(w.nimg.as<float2>(), n, acc);
+        check_launch("norm2");
+        double nn = 0;
+        MMR_CUDA(cudaMemcpyAsync(&nn, acc, sizeof(double), cudaMemcpyDeviceToHost, st));
+        MMR_CUDA(cudaStreamSynchronize(st));
+        h.stop_thresh = o.nse_thresh_fact * nn;
+        h.has_stop = 1;
+    }
+    const double stop_thresh_out = h.has_stop ? h.stop_thresh : NAN;
+    MMR_CUDA(cudaMemcpyAsync(w.state.p, &h, sizeof(CgState), cudaMemcpyHostToDevice, st));
+    MMR_CUDA(cudaMemsetAsync(w.hist.p, 0, (size_t)4 * cap * sizeof(double), st));
+    CgState* sp = w.state.as<CgState>();
+    // initial residual (164-181)
+    sense_normal(a, w.x.as<float2>(), w.tmp.as<float2>(), st, nullptr);
+    cg_init_kernel<<<red_grid(n), 256, 0, st>>>(w.b.as<float2>(), w.tmp.as<float2>(), w.x.as<float2>(),
+                                               has_tik ? w.tik.as<float>() : nullptr,
+                                               has_gt ? w.gt.as<float2>() : nullptr, w.res.as<float2>(),
+                                               w.p.as<float2>(), n, sp, w.hist.as<double>());
+    check_launch("cg_init");
+
+    // graphs (re-captured when buffers or options that change kernel arguments differ)
+    const void* key[8] = {a.d_wnorm.p, a.s_grid.p, a.s_grid2.p, w.x.p, w.hist.p, (const void*)(intptr_t)has_tik,
+                          (const void*)(intptr_t)has_gt, a.nufft ? a.nufft->s_tmp.p : nullptr};
+    const long long keyv[4] = {a.w_bstride, sense_chunk(a), a.nufft && a.nufft->use_bins ? a.nufft->bins.T : 0, cap};
+    bool same = w.g_norm != nullptr;
+    for (int i = 0; i < 8 && same; ++i) same = key[i] == w.key[i];
+    for (int i = 0; i < 4 && same; ++i) same = keyv[i] == w.keyv[i];
+    if (!same) {
+        if (w.g_norm) cudaGraphExecDestroy(w.g_norm);
+        if (w.g_expl) cudaGraphExecDestroy(w.g_expl);
+        w.g_norm = w.g_expl = nullptr;
+        // one eager normal op sizes every scratch buffer before capture
+        w.g_norm = capture_iter(a, w, false, has_tik, has_gt);
+        w.g_expl = capture_iter(a, w, true, has_tik, has_gt);
+        for (int i = 0; i < 8; ++i) w.key[i] = key[i];
+        for (int i = 0; i < 4; ++i) w.keyv[i] = keyv[i];
+    }
+    const int expResN = std::max(1, o.exp_res_n);
+    const bool dynamic = h.has_resThresh || h.has_resChange || h.has_xChange || h.has_stop || h.stopOnResInc > 0 ||
+                         h.stopOnXdifInc > 0;
+    const int limit = nitmax0 + (h.has_stop ? extra : 0);
+    const int poll = dynamic ? 4 : limit;
+    int it = 0;
+    while (it < limit) {
+        const int end = std::min(limit, it + poll);
+        for (; it < end; ++it) MMR_CUDA(cudaGraphLaunch((it % expResN == 0) ? w.g_expl : w.g_norm, st));
+        int fin = 0;
+        MMR_CUDA(cudaMemcpyAsync(&fin, &sp->finished, sizeof(int), cudaMemcpyDeviceToHost, st));
+        MMR_CUDA(cudaStreamSynchronize(st));
+        if (fin) break;
+    }
+    CgState fs;
+    MMR_CUDA(cudaMemcpyAsync(&fs, sp, sizeof(CgState), cudaMemcpyDeviceToHost, st));
+    float2* xo = (float2*)stage_out(w.sxo, x_user, n * 8);
+    MMR_CUDA(cudaMemcpyAsync(xo, w.x.p, n * 8, cudaMemcpyDeviceToDevice, st));
+    finish_out(w.sxo, n * 8, st);
+    MMR_CUDA(cudaStreamSynchronize(st));
+    if (hist) {
+        hist->nit = fs.nit;
+        hist->n = fs.nit + 1;
+        hist->status = fs.status;
+        hist->stop_thresh = stop_thresh_out;
+        const int m = std::min(hist->capacity, fs.nit + 1);
+        std::vector<double> hh((size_t)4 * cap);
+        MMR_CUDA(cudaMemcpy(hh.data(), w.hist.p, hh.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        for (int i = 0; i < m; ++i) {
+            if (hist->res_sq) hist->res_sq[i] = hh[i];
+            if (hist->mse) hist->mse[i] = hh[cap + i];
+            if (hist->xnorm) hist->xnorm[i] = hh[2 * cap + i];
+            if (hist->xdiff) hist->xdiff[i] = hh[3 * cap + i];
+        }
+    }
+    MMR_CUDA(cudaEventRecord(ev, st));
+    MMR_CUDA(cudaStreamWaitEvent(ust, ev, 0));
+    cudaEventDestroy(ev);
+    if (device_error_word(st)) MMR_THROW(MMR_ERR_TIMEOUT, "a bounded device wait ran out during cgne");
+}
+
+}  // namespace mmr
+
+using namespace mmr;
+
+extern "C" int mmr_cgne_default_opts(mmr_cgne_opts* o) {
+    return guarded([&] {
+        MMR_REQUIRE(o, "NULL opts");
+        memset(o, 0, sizeof(*o));
+        o->nit_max = 1000;
+        o->res_thresh = 1e-10;
+        o->res_change_thresh = NAN;
+        o->x_change_thresh = 1e-10;
+        o->exp_res_n = 100;
+        o->nse_thresh_fact = 1.0;
+        o->nse_extra_it = 4;
+        o->stop_on_res_inc = 0;
+        o->res_inc_thresh = 1.0;
+        o->stop_on_xdif_inc = 0;
+        o->noise_var = NAN;
+        o->want_history = 1;
+    });
+}
+
+extern "C" int mmr_cgne_solve(mmr_sense* A, const void* b, const void* x0, const float* W, const mmr_cgne_opts* opts,
+                              void* x_out, mmr_cgne_hist* hist, void* stream) {
+    return guarded([&] {
+        MMR_REQUIRE(A && b && x_out, "NULL argument");
+        mmr_cgne_opts o;
+        if (opts) o = *opts;
+        else mmr_cgne_default_opts(&o);
+        cg_solve(A->a, b, x0, W, o, x_out, hist, as_stream(stream));
+    });
+}

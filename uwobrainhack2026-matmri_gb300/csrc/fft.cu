@@ -1,0 +1,226 @@
+// FFT pass kernels: Stockham radix stages in shared memory with fused
+// prologue (deapodisation, coil-map multiply, zero padding) and epilogue
+// (crop, deapodisation, conj-map multiply and a deterministic coil sum
+// across a thread-block cluster through distributed shared memory).
+#include <cmath>
+#include <map>
+#include <mutex>
+
+#include "fft.cuh"
+
+namespace cg = cooperative_groups;
+
+namespace mmr {
+
+FftFactors fft_factorize(int L) {
+    FftFactors f;
+    f.L = L;
+    int n = L;
+    std::vector<int> r;
+    while (n % 8 == 0) { r.push_back(8); n /= 8; }
+    while (n % 4 == 0) { r.push_back(4); n /= 4; }
+    while (n % 2 == 0) { r.push_back(2); n /= 2; }
+    while (n % 3 == 0) { r.push_back(3); n /= 3; }
+    while (n % 5 == 0) { r.push_back(5); n /= 5; }
+    while (n % 7 == 0) { r.push_back(7); n /= 7; }
+    MMR_REQUIRE(n == 1, "FFT length %d has a prime factor > 7", L);
+    MMR_REQUIRE((int)r.size() <= FFT_MAX_STAGES, "FFT length %d needs too many stages", L);
+    f.nstage = (int)r.size();
+    for (int i = 0; i < f.nstage; ++i) f.radix[i] = r[i];
+    return f;
+}
+
+const float2* fft_twiddles(int L) {
+    static std::mutex mu;
+    static std::map<std::pair<int, int>, float2*> cache;   // (device, L)
+    int dev = 0;
+    MMR_CUDA(cudaGetDevice(&dev));
+    std::lock_guard<std::mutex> g(mu);
+    auto it = cache.find({dev, L});
+    if (it != cache.end()) return it->second;
+    std::vector<float2> h(L);
+    for (int m = 0; m < L; ++m) {
+        // e^{-2 pi i m / L} in FP64, exact at the quarter points
+        const double a = -2.0 * M_PI * (double)m / (double)L;
+        h[m] = make_float2((float)std::cos(a), (float)std::sin(a));
+        if (4 * m % L == 0) {
+            const int q = (4 * m / L) & 3;
+            const float c[4] = {1.f, 0.f, -1.f, 0.f}, s[4] = {0.f, -1.f, 0.f, 1.f};
+            h[m] = make_float2(c[q], s[q]);
+        }
+    }
+    float2* d = nullptr;
+    MMR_CUDA(cudaMalloc(&d, L * sizeof(float2)));
+    MMR_CUDA(cudaMemcpy(d, h.data(), L * sizeof(float2), cudaMemcpyHostToDevice));
+    cache[{dev, L}] = d;
+    return d;
+}
+
+template <int MODE, int SIGN>
+__global__ void __launch_bounds__(256) fft_pass_kernel(const PassArgs a) {
+    extern __shared__ float4 sm4[];
+    float2* sm = reinterpret_cast<float2*>(sm4);
+    if (a.active && *a.active) return;
+    const int L = a.L, B = a.B, ls = L;
+    float2* buf0 = sm;
+    float2* buf1 = sm + B * ls;
+    float2* twd = sm + 2 * B * ls;
+    const int tid = threadIdx.x, nt = blockDim.x;
+    for (int i = tid; i < L; i += nt) twd[i] = a.tw[i];
+
+    // ---- tile decomposition
+    const bool contiguous = (MODE != PASS_ADJ_COMBINE) && a.inner == 1;
+    long long l0 = 0, q0 = 0, o = 0;
+    int coil = 0;
+    if (contiguous) {
+        l0 = (long long)blockIdx.x * B;
+    } else {
+        const long long ntq = (a.inner + B - 1) / B;
+        o = (MODE == PASS_ADJ_COMBINE) ? 0 : (long long)blockIdx.x / ntq;
+        q0 = ((long long)blockIdx.x % ntq) * B;
+        if (MODE == PASS_ADJ_COMBINE) coil = blockIdx.y;
+    }
+    auto line_valid = [&](int b) -> bool {
+        return contiguous ? (l0 + b < a.outer) : (q0 + b < a.inner);
+    };
+
+    // ---- zero the positions that carry no input (zero padding)
+    const int nz = L - a.nin;
+    for (int idx = tid; idx < B * nz; idx += nt) {
+        const int b = idx / nz, t = a.nin + idx % nz;
+        int nat = a.in_start + t;
+        nat -= (nat >= L) ? L : 0;
+        buf0[b * ls + nat] = make_float2(0.f, 0.f);
+    }
+    // ---- load (coalesced along the contiguous index)
+    for (int idx = tid; idx < B * a.nin; idx += nt) {
+        int b, t;
+        if (contiguous) { b = idx / a.nin; t = idx - b * a.nin; }
+        else { t = idx / B; b = idx - t * B; }
+        float2 v = make_float2(0.f, 0.f);
+        if (line_valid(b)) {
+            if (MODE == PASS_FWD_IMG) {
+                const long long l = l0 + b;
+                const float2 x = a.in[t + (long long)a.nin * (l % a.lpc)];
+                v = a.maps ? cmul(x, a.maps[t + (long long)a.nin * l]) : x;
+            } else if (contiguous) {
+                v = a.in[t + (long long)a.nin * (l0 + b)];
+            } else {
+                const long long oo = (MODE == PASS_ADJ_COMBINE) ? coil : o;
+                v = a.in[(q0 + b) + a.inner * (t + (long long)a.nin * oo)];
+            }
+            if (a.in_fac) v = cmul(v, a.in_fac[t]);
+        }
+        int nat = a.in_start + t;
+        nat -= (nat >= L) ? L : 0;
+        buf0[b * ls + nat] = v;
+    }
+    __syncthreads();
+
+    float2* res = fft_lines<SIGN>(buf0, buf1, twd, a.f, B, ls);
+    float2* spare = (res == buf0) ? buf1 : buf0;
+
+    if (MODE != PASS_ADJ_COMBINE) {
+        for (int idx = tid; idx < B * a.nout; idx += nt) {
+            int b, t;
+            if (contiguous) { b = idx / a.nout; t = idx - b * a.nout; }
+            else { t = idx / B; b = idx - t * B; }
+            if (!line_valid(b)) continue;
+            int nat = a.out_start + t;
+            nat -= (nat >= L) ? L : 0;
+            float2 v = cscale(res[b * ls + nat], a.scale);
+            if (a.out_fac) v = cmul(v, a.out_fac[t]);
+            if (contiguous) a.out[t + (long long)a.nout * (l0 + b)] = v;
+            else a.out[(q0 + b) + a.inner * (t + (long long)a.nout * o)] = v;
+        }
+        return;
+    }
+
+    // ---- ADJ_COMBINE: conj-map multiply, then deterministic coil sum over the cluster
+    for (int idx = tid; idx < B * a.nout; idx += nt) {
+        const int t = idx / B, b = idx - t * B;
+        float2 v = make_float2(0.f, 0.f);
+        if (line_valid(b)) {
+            int nat = a.out_start + t;
+            nat -= (nat >= L) ? L : 0;
+            v = cscale(res[b * ls + nat], a.scale);
+            if (a.out_fac) v = cmul(v, a.out_fac[t]);
+            if (a.maps) v = cmulc(v, a.maps[(q0 + b) + a.inner * (t + (long long)a.nout * coil)]);
+        }
+        spare[idx] = v;
+    }
+    cg::cluster_group cl = cg::this_cluster();
+    cl.sync();
+    const int cs = (int)cl.num_blocks();
+    const int rank = (int)cl.block_rank();
+    const int tot = B * a.nout;
+    const int per = (tot + cs - 1) / cs;
+    const int e0 = rank * per, e1 = min(tot, e0 + per);
+    for (int idx = e0 + tid; idx < e1; idx += nt) {
+        float2 s = make_float2(0.f, 0.f);
+        for (int r = 0; r < cs; ++r) {
+            const float2* rem = cl.map_shared_rank(spare, r);
+            s = cadd(s, rem[idx]);
+        }
+        const int t = idx / B, b = idx - t * B;
+        if (q0 + b < a.inner) {
+            float2* dst = a.out + (q0 + b) + a.inner * (long long)t;
+            *dst = a.accumulate ? cadd(*dst, s) : s;
+        }
+    }
+    cl.sync();
+}
+
+template <int MODE, int SIGN>
+static void launch_mode(const PassArgs& a, cudaStream_t st) {
+    const size_t smem = (size_t)(2 * a.B * a.L + a.L) * sizeof(float2);
+    auto kern = fft_pass_kernel<MODE, SIGN>;
+    static bool attr_done = false;   // one per instantiation
+    if (!attr_done) {
+        MMR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
+        if (MODE == PASS_ADJ_COMBINE)
+            MMR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
+        attr_done = true;
+    }
+    const bool contiguous = (MODE != PASS_ADJ_COMBINE) && a.inner == 1;
+    long long nblk;
+    if (contiguous) nblk = (a.outer + a.B - 1) / a.B;
+    else nblk = ((a.inner + a.B - 1) / a.B) * ((MODE == PASS_ADJ_COMBINE) ? 1 : a.outer);
+    MMR_REQUIRE(nblk < (1LL << 31), "FFT pass grid too large");
+    if (nblk == 0) return;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    if (MODE == PASS_ADJ_COMBINE) {
+        const int cs = (int)a.outer;     // coils in the cluster
+        cfg.gridDim = dim3((unsigned)nblk, (unsigned)cs);
+        attr[0].id = cudaLaunchAttributeClusterDimension;
+        attr[0].val.clusterDim.x = 1;
+        attr[0].val.clusterDim.y = cs;
+        attr[0].val.clusterDim.z = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+    } else {
+        cfg.gridDim = dim3((unsigned)nblk);
+        cfg.numAttrs = 0;
+    }
+    MMR_CUDA(cudaLaunchKernelEx(&cfg, kern, a));
+}
+
+void launch_fft_pass(int mode, const PassArgs& a, cudaStream_t st) {
+    MMR_REQUIRE(a.nin <= a.L && a.nout <= a.L && a.nin > 0 && a.nout > 0, "bad FFT pass extents");
+    if (mode == PASS_ADJ_COMBINE) MMR_REQUIRE(a.outer >= 1 && a.outer <= 16, "cluster coil count must be 1..16");
+    if (a.sign < 0) {
+        if (mode == PASS_PLAIN) launch_mode<PASS_PLAIN, -1>(a, st);
+        else if (mode == PASS_FWD_IMG) launch_mode<PASS_FWD_IMG, -1>(a, st);
+        else launch_mode<PASS_ADJ_COMBINE, -1>(a, st);
+    } else {
+        if (mode == PASS_PLAIN) launch_mode<PASS_PLAIN, 1>(a, st);
+        else if (mode == PASS_FWD_IMG) launch_mode<PASS_FWD_IMG, 1>(a, st);
+        else launch_mode<PASS_ADJ_COMBINE, 1>(a, st);
+    }
+}
+
+}  // namespace mmr

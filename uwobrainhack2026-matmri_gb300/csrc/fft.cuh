@@ -1,0 +1,199 @@
+// Hand-written mixed-radix Stockham FFT passes in shared memory (sm_103a).
+//
+// A "pass" transforms every line of an array along one axis.  The array is
+// viewed as [inner, n_axis, outer] (column-major: `inner` is the product of
+// the dims before the axis, `outer` the product after it).  Input position
+// t < nin holds natural index (in_start + t) mod L; output position t < nout
+// takes natural index (out_start + t) mod L.  This expresses, without data
+// movement, the zero padding "at the end" of ifftnc(..., sz) (general/ifftnc.m:102-104),
+// the crop 1:imN of nufftOp.m:366-372, the image-centering phase ramp
+// fftShiftArray (nufftOp.m:258-272, a pure index shift of N/2 plus the
+// constant exp(i*pi*N/2)), and the fft-shifted ("centered") storage of the
+// oversampled grid used by the gridding kernels.
+#pragma once
+
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+
+#include "common.h"
+
+namespace mmr {
+
+constexpr int FFT_MAX_STAGES = 12;
+
+struct FftFactors {
+    int L = 0;
+    int nstage = 0;
+    int radix[FFT_MAX_STAGES] = {0};
+};
+
+FftFactors fft_factorize(int L);            // radices from {8,4,2,3,5,7}
+const float2* fft_twiddles(int L);          // device table e^{-2 pi i m / L}, m < L (cached)
+
+enum PassMode : int {
+    PASS_PLAIN = 0,     // value = in[...] * in_fac[t]
+    PASS_FWD_IMG = 1,   // value = img[t, line % lpc] * maps[t, c0*lpc + line] * in_fac[t]
+    PASS_ADJ_COMBINE = 2 // out[q, t] (+)= sum_c fft(...)[t] * out_fac[t] * conj(maps[q, t, c])
+};
+
+struct PassArgs {
+    const float2* in = nullptr;
+    float2* out = nullptr;
+    const float2* maps = nullptr;   // FWD_IMG / ADJ_COMBINE
+    const float2* in_fac = nullptr; // per input position (nullable)
+    const float2* out_fac = nullptr;// per output position (nullable)
+    const float2* tw = nullptr;
+    const int* active = nullptr;    // solver "finished" flag: skip when *active != 0
+    long long inner = 1;            // product of dims before the axis
+    long long outer = 1;            // product of dims after the axis (lines = inner*outer)
+    long long lpc = 1;              // FWD_IMG: lines per coil (image lines)
+    int L = 0;
+    int nin = 0, in_start = 0;
+    int nout = 0, out_start = 0;
+    int sign = -1;                  // -1: e^{-i} (fft), +1: e^{+i} (ifft)
+    float scale = 1.f;
+    int B = 1;                      // lines per block
+    int accumulate = 0;             // ADJ_COMBINE: out += (1) or out = (0)
+    FftFactors f;
+};
+
+// ------------------------------------------------------------ complex math ----
+__device__ __forceinline__ float2 cmul(float2 a, float2 b) {
+    return make_float2(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x);
+}
+__device__ __forceinline__ float2 cmulc(float2 a, float2 b) {   // a * conj(b)
+    return make_float2(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y);
+}
+__device__ __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+// multiply by sign*i  (sign = -1 -> -i, +1 -> +i)
+__device__ __forceinline__ float2 cmul_si(float2 a, int sign) {
+    return sign < 0 ? make_float2(a.y, -a.x) : make_float2(-a.y, a.x);
+}
+
+// ------------------------------------------------------------- butterflies ----
+template <int SIGN>
+__device__ __forceinline__ void dft2(float2& a, float2& b) {
+    float2 t = a;
+    a = cadd(t, b);
+    b = csub(t, b);
+}
+
+template <int SIGN>
+__device__ __forceinline__ void dft4(float2* v) {
+    float2 a0 = cadd(v[0], v[2]), a1 = csub(v[0], v[2]);
+    float2 a2 = cadd(v[1], v[3]), a3 = cmul_si(csub(v[1], v[3]), SIGN);
+    v[0] = cadd(a0, a2);
+    v[2] = csub(a0, a2);
+    v[1] = cadd(a1, a3);
+    v[3] = csub(a1, a3);
+}
+
+template <int SIGN>
+__device__ __forceinline__ void dft8(float2* v) {
+    const float h = 0.70710678118654752440f;
+    float2 e[4] = {v[0], v[2], v[4], v[6]};
+    float2 o[4] = {v[1], v[3], v[5], v[7]};
+    dft4<SIGN>(e);
+    dft4<SIGN>(o);
+    // twiddles w8^k, k = 0..3, w8 = e^{SIGN i pi/4}
+    float2 t1 = make_float2(h * (o[1].x - SIGN * o[1].y), h * (o[1].y + SIGN * o[1].x));
+    float2 t2 = cmul_si(o[2], SIGN);
+    float2 t3 = make_float2(h * (-o[3].x - SIGN * o[3].y), h * (-o[3].y + SIGN * o[3].x));
+    v[0] = cadd(e[0], o[0]);
+    v[4] = csub(e[0], o[0]);
+    v[1] = cadd(e[1], t1);
+    v[5] = csub(e[1], t1);
+    v[2] = cadd(e[2], t2);
+    v[6] = csub(e[2], t2);
+    v[3] = cadd(e[3], t3);
+    v[7] = csub(e[3], t3);
+}
+
+// Direct DFT for the odd radices 3, 5, 7 (constants from cospi/sinpi).
+template <int R, int SIGN>
+__device__ __forceinline__ void dft_odd(float2* v) {
+    float2 outv[R];
+#pragma unroll
+    for (int k = 0; k < R; ++k) {
+        float2 acc = v[0];
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+            const int m = (r * k) % R;
+            const float c = cospif(2.0f * m / R);
+            const float s = SIGN * sinpif(2.0f * m / R);
+            acc.x += v[r].x * c - v[r].y * s;
+            acc.y += v[r].x * s + v[r].y * c;
+        }
+        outv[k] = acc;
+    }
+#pragma unroll
+    for (int k = 0; k < R; ++k) v[k] = outv[k];
+}
+
+template <int R, int SIGN>
+__device__ __forceinline__ void dftR(float2* v) {
+    if constexpr (R == 2) dft2<SIGN>(v[0], v[1]);
+    else if constexpr (R == 4) dft4<SIGN>(v);
+    else if constexpr (R == 8) dft8<SIGN>(v);
+    else dft_odd<R, SIGN>(v);
+}
+
+// One Stockham stage for all B lines held in `src` (line stride `ls`), into `dst`.
+template <int R, int SIGN>
+__device__ __forceinline__ void stockham_stage(const float2* __restrict__ src, float2* __restrict__ dst,
+                                               const float2* __restrict__ tw, int L, int Ns, int B, int ls) {
+    const int nbf = L / R;
+    const int tws = L / (Ns * R);
+    for (int w = threadIdx.x; w < nbf * B; w += blockDim.x) {
+        const int b = w / nbf;
+        const int j = w - b * nbf;
+        const int k = j % Ns;
+        const float2* s = src + b * ls;
+        float2 v[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[r] = s[j + r * nbf];
+        if (Ns > 1) {
+#pragma unroll
+            for (int r = 1; r < R; ++r) {
+                float2 t = tw[r * k * tws];
+                if (SIGN > 0) t.y = -t.y;
+                v[r] = cmul(v[r], t);
+            }
+        }
+        dftR<R, SIGN>(v);
+        float2* d = dst + b * ls + (j / Ns) * Ns * R + k;
+#pragma unroll
+        for (int r = 0; r < R; ++r) d[r * Ns] = v[r];
+    }
+}
+
+// Runs all stages; returns the buffer (a or b) holding the result.
+template <int SIGN>
+__device__ float2* fft_lines(float2* a, float2* b, const float2* tw, const FftFactors& f, int B, int ls) {
+    int Ns = 1;
+    for (int s = 0; s < f.nstage; ++s) {
+        const int R = f.radix[s];
+        switch (R) {
+            case 8: stockham_stage<8, SIGN>(a, b, tw, f.L, Ns, B, ls); break;
+            case 4: stockham_stage<4, SIGN>(a, b, tw, f.L, Ns, B, ls); break;
+            case 2: stockham_stage<2, SIGN>(a, b, tw, f.L, Ns, B, ls); break;
+            case 3: stockham_stage<3, SIGN>(a, b, tw, f.L, Ns, B, ls); break;
+            case 5: stockham_stage<5, SIGN>(a, b, tw, f.L, Ns, B, ls); break;
+            case 7: stockham_stage<7, SIGN>(a, b, tw, f.L, Ns, B, ls); break;
+            default: break;
+        }
+        __syncthreads();
+        float2* t = a;
+        a = b;
+        b = t;
+        Ns *= R;
+    }
+    return a;
+}
+
+// Launch a pass (host). `cluster` > 1 only for PASS_ADJ_COMBINE.
+void launch_fft_pass(int mode, const PassArgs& a, cudaStream_t st);
+
+}  // namespace mmr

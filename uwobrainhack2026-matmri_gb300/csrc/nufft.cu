@@ -1,0 +1,1045 @@
+// @nufftOp on GB300: FP64 plan precompute (host) and the gridding kernels.
+//
+// Plan (operators/@nufftOp/nufftOp.m:138-274): oversampled size osN, the
+// tabulated Kaiser-Bessel kernel with linear table interpolation, the
+// deapodisation comp, per-sample tap weights and base cells.  The sparse
+// interpolation matrix convMat (nufftOp.m:257) is never materialised: each
+// sample keeps its base cell floor((k+0.5) osN) and its separable per-dim tap
+// weights, exactly the factors whose products are convMat's entries.
+//
+// Gridding (nufftOp.m:359 convMat'*y and nufftOp.m:389 convMat*y):
+//  * interp2d_binned  — forward interpolation; each CTA stages one grid tile
+//    plus halo for a group of coils into shared memory with a TMA tensor
+//    copy (cp.async.bulk.tensor.3d, mbarrier completion, bounded wait) and
+//    evaluates the W x W taps of a sample with one lane per tap and a
+//    warp-shuffle reduction;
+//  * spread2d_binned  — adjoint spreading; samples are pre-sorted into the
+//    tiles their footprint touches, each CTA owns one output tile,
+//    accumulates it in shared memory and flushes it with coalesced stores
+//    (no global atomics, no memset of the grid);
+//  * gridnorm2d_binned — the two fused for the normal operator
+//    C^H diag(w) C: interp from a staged tile + 2W halo, weight, spread into
+//    the owned tile; the samples never round-trip through HBM;
+//  * interp_generic / spread_generic — any ndim / small grids.
+#include <algorithm>
+#include <cmath>
+#include <cudaTypedefs.h>
+
+#include "nufft.cuh"
+
+namespace mmr {
+
+__device__ int g_dev_error = 0;
+
+int device_error_word(cudaStream_t st) {
+    int v = 0;
+    MMR_CUDA(cudaMemcpyFromSymbolAsync(&v, g_dev_error, sizeof(int), 0, cudaMemcpyDeviceToHost, st));
+    MMR_CUDA(cudaStreamSynchronize(st));
+    if (v) {
+        int z = 0;
+        MMR_CUDA(cudaMemcpyToSymbol(g_dev_error, &z, sizeof(int)));
+    }
+    return v;
+}
+
+// ----------------------------------------------------------------- host plan --
+static int max_prime_factor(int n) {
+    int f = 1;
+    for (int p = 2; p * p <= n; ++p)
+        while (n % p == 0) { f = p; n /= p; }
+    return n > 1 ? std::max(f, n) : f;
+}
+
+// I0 by its power series (positive terms); matches besseli(0,.) to ~1e-15 here.
+static double bessel_i0(double z) {
+    const double q = z * z / 4.0;
+    double term = 1.0, acc = 1.0;
+    for (int k = 1; k < 500; ++k) {
+        term *= q / ((double)k * (double)k);
+        acc += term;
+        if (term <= 1e-17 * acc) break;
+    }
+    return acc;
+}
+
+static inline long long imod(long long a, long long m) {
+    long long r = a % m;
+    return r < 0 ? r + m : r;
+}
+
+void nufft_plan_build(NufftPlan& p, const mmr_nufft_desc& d) {
+    MMR_REQUIRE(d.ndim >= 1 && d.ndim <= 3, "ndim must be 1..3 (got %d)", d.ndim);
+    MMR_REQUIRE(d.nsamp >= 1, "need at least one sample");
+    MMR_REQUIRE(d.kloc != nullptr, "kloc is NULL");
+    p.nd = d.ndim;
+    p.M = d.nsamp;
+    p.os = d.os > 0 ? d.os : 1.5;                  // nufftOp.m:66
+    p.W = d.kwidth > 0 ? d.kwidth : 6;             // nufftOp.m:65
+    MMR_REQUIRE(p.W % 2 == 0 && p.W >= 2 && p.W <= 8, "kwidth must be even in 2..8 (got %d)", p.W);
+    const double barg = p.W * (double)p.W / (p.os * p.os) * (p.os - 0.5) * (p.os - 0.5) - 0.8;
+    MMR_REQUIRE(barg > 0, "kwidth/os combination gives a non-real Kaiser-Bessel beta");
+    p.beta = M_PI * std::sqrt(barg);                                                 // 155
+    p.Nkern = (int)(std::ceil(0.5 * (p.W + 1) * std::sqrt(0.37 / (p.os * p.os) / 1e-6)) * 2);   // 156
+    p.Ntot = p.Gtot = 1;
+    for (int k = 0; k < 3; ++k) { p.N[k] = 1; p.G[k] = 1; }
+    for (int k = 0; k < p.nd; ++k) {
+        MMR_REQUIRE(d.imN[k] >= 2 && d.imN[k] % 2 == 0 && d.imN[k] <= 32768,
+                    "imN(%d) = %lld must be even in [2, 32768]", k + 1, (long long)d.imN[k]);
+        p.N[k] = (int)d.imN[k];
+        int g = (int)(std::ceil(p.N[k] * p.os / 2.0) * 2);                            // 146
+        while (max_prime_factor(g) > 7) g += 2;                                       // 148-152
+        MMR_REQUIRE(g >= p.N[k] && g >= 2 * p.W, "oversampled size %d too small", g);
+        p.G[k] = g;
+        p.Ntot *= p.N[k];
+        p.Gtot *= g;
+    }
+    p.kloc.assign(d.kloc, d.kloc + p.M * p.nd);
+    for (double v : p.kloc) MMR_REQUIRE(std::isfinite(v), "kloc holds NaN/Inf");
+
+    // kernel table (157-165)
+    const int Nk = p.Nkern;
+    std::vector<double> kern(Nk + 1);
+    double ksum = 0;
+    for (int i = 0; i < Nk; ++i) {
+        const double kx = -1.0 + 2.0 * i / (Nk - 1);
+        kern[i] = bessel_i0(p.beta * std::sqrt(std::max(0.0, 1.0 - kx * kx)));
+        ksum += kern[i];
+    }
+    kern[Nk] = 0.0;
+    for (auto& v : kern) v = v / ksum * (double)(Nk - 1) / p.W;
+
+    // deapodisation (171-181) and the fftShiftArray constant exp(+-i pi N/2)
+    for (int k = 0; k < p.nd; ++k) {
+        const int n = p.N[k], g = p.G[k];
+        std::vector<double> c(n);
+        int imin = 0;
+        for (int i = 0; i < n; ++i) {
+            const double x0 = (i - n / 2) * M_PI * p.W / g;
+            const double z = x0 * x0 - p.beta * p.beta;
+            double v;
+            if (z < 0) { const double y = std::sqrt(-z); v = y / std::sinh(y); }
+            else if (z > 0) { const double x = std::sqrt(z); v = x / std::sin(x); }
+            else v = 1.0;
+            c[i] = v;
+            if (std::fabs(v) < std::fabs(c[imin])) imin = i;
+        }
+        const double cm = c[imin], sc = std::sqrt((double)g / n);
+        const double ph = M_PI * n / 2.0;
+        std::vector<float2> ff(n), fa(n);
+        for (int i = 0; i < n; ++i) {
+            const double v = c[i] / cm * sc;
+            ff[i] = make_float2((float)(v * std::cos(ph)), (float)(v * std::sin(ph)));
+            fa[i] = make_float2((float)(v * std::cos(ph)), (float)(-v * std::sin(ph)));
+        }
+        p.d_fwd_fac[k].upload(ff);
+        p.d_adj_fac[k].upload(fa);
+        p.ff[k] = fft_factorize(g);
+        p.tw[k] = fft_twiddles(g);
+    }
+
+    // per-sample base cells and tap weights (216-238)
+    std::vector<int> base((size_t)p.nd * p.M);
+    std::vector<float> wts((size_t)p.M * p.nd * p.W);
+    for (long long s = 0; s < p.M; ++s) {
+        for (int k = 0; k < p.nd; ++k) {
+            const double ka = p.kloc[s + p.M * k] + 0.5;                   // 141
+            const double xa = ka * p.G[k];                                 // 217
+            const double fl = std::floor(xa);
+            const double kia = fl - xa;                                    // 218
+            base[(size_t)k * p.M + s] = (int)imod((long long)fl, p.G[k]);
+            for (int t = 0; t < p.W; ++t) {
+                const double off = -p.W / 2 + 1 + t;
+                double ki = (kia + off) * (Nk - 1) / p.W + Nk / 2.0 + 0.5; // 220-221
+                const double fi = std::floor(ki);
+                const double frac = ki - fi;                               // 222
+                long long idx = (long long)fi;                             // 1-based (223)
+                idx = std::min<long long>(std::max<long long>(idx, 1), Nk);
+                const double w = (1.0 - frac) * kern[idx - 1] + frac * kern[idx];   // 225
+                wts[((size_t)s * p.nd + k) * p.W + t] = (float)w;
+            }
+        }
+    }
+    p.d_base.upload(base);
+    p.d_w.upload(wts);
+    nufft_set_dcf(p, d.dcf);
+    if (p.nd == 2) nufft_build_bins(p, 32);
+}
+
+void nufft_set_dcf(NufftPlan& p, const double* dcf) {
+    p.dcf_version++;
+    if (!dcf) {
+        p.has_dcf = false;
+        p.dcf_h.clear();
+        return;
+    }
+    p.dcf_h.assign(dcf, dcf + p.M);
+    std::vector<float> f(p.M);
+    for (long long s = 0; s < p.M; ++s) {
+        MMR_REQUIRE(std::isfinite(dcf[s]), "dcf holds NaN/Inf");
+        f[s] = (float)dcf[s];
+    }
+    p.d_dcf.upload(f);
+    p.has_dcf = true;
+}
+
+void nufft_build_bins(NufftPlan& p, int Treq) {
+    p.use_bins = false;
+    if (p.nd != 2) return;
+    int T = Treq;
+    while (T >= 8 && (p.G[0] < 2 * (T + 2 * p.W) || p.G[1] < 2 * (T + 2 * p.W))) T /= 2;
+    if (T < 8 || T < p.W) return;
+    BinLists& b = p.bins;
+    b.T = T;
+    b.ntx = (int)cdiv(p.G[0], T);
+    b.nty = (int)cdiv(p.G[1], T);
+    const int ntile = b.ntx * b.nty;
+    std::vector<int> base((size_t)2 * p.M);
+    MMR_CUDA(cudaMemcpy(base.data(), p.d_base.p, base.size() * sizeof(int), cudaMemcpyDeviceToHost));
+    const int off0 = -p.W / 2 + 1;
+    auto sdist = [](long long a, int g) {   // signed representative of a mod g in [-g/2, g/2)
+        long long r = imod(a, g);
+        return (int)(r >= g / 2 ? r - g : r);
+    };
+    // own lists
+    std::vector<int> cnt(ntile + 1, 0);
+    for (long long s = 0; s < p.M; ++s) {
+        const int c1 = base[s], c2 = base[p.M + s];
+        cnt[(c2 / T) * b.ntx + c1 / T + 1]++;
+    }
+    for (int t = 0; t < ntile; ++t) cnt[t + 1] += cnt[t];
+    std::vector<int> own_s(p.M), pos(cnt.begin(), cnt.end() - 1);
+    std::vector<short2> own_lb(p.M);
+    b.max_own = 0;
+    for (int t = 0; t < ntile; ++t) b.max_own = std::max(b.max_own, cnt[t + 1] - cnt[t]);
+    for (long long s = 0; s < p.M; ++s) {
+        const int c1 = base[s], c2 = base[p.M + s];
+        const int tx = c1 / T, ty = c2 / T, t = ty * b.ntx + tx;
+        const int e = pos[t]++;
+        own_s[e] = (int)s;
+        own_lb[e] = make_short2((short)(c1 - tx * T), (short)(c2 - ty * T));
+    }
+    b.own_ptr.upload(cnt);
+    b.own_s.upload(own_s);
+    b.own_lb.upload(own_lb);
+    b.n_own = p.M;
+    // padded lists: every tile touched by the footprint
+    std::vector<std::vector<int>> tiles_s(ntile);
+    std::vector<std::vector<short2>> tiles_lb(ntile);
+    for (long long s = 0; s < p.M; ++s) {
+        const int c[2] = {base[s], base[p.M + s]};
+        int tl[2][8], ntl[2] = {0, 0};
+        for (int k = 0; k < 2; ++k) {
+            for (int j = 0; j < p.W; ++j) {
+                const int u = (int)imod(c[k] + off0 + j, p.G[k]);
+                const int ti = u / T;
+                bool seen = false;
+                for (int q = 0; q < ntl[k]; ++q) seen |= (tl[k][q] == ti);
+                if (!seen) tl[k][ntl[k]++] = ti;
+            }
+        }
+        for (int a = 0; a < ntl[0]; ++a)
+            for (int bb = 0; bb < ntl[1]; ++bb) {
+                const int tx = tl[0][a], ty = tl[1][bb], t = ty * b.ntx + tx;
+                tiles_s[t].push_back((int)s);
+                tiles_lb[t].push_back(make_short2((short)sdist((long long)c[0] - (long long)tx * T, p.G[0]),
+                                                  (short)sdist((long long)c[1] - (long long)ty * T, p.G[1])));
+            }
+    }
+    std::vector<int> pptr(ntile + 1, 0), ps;
+    std::vector<short2> plb;
+    b.max_pad = 0;
+    for (int t = 0; t < ntile; ++t) {
+        pptr[t + 1] = pptr[t] + (int)tiles_s[t].size();
+        b.max_pad = std::max(b.max_pad, (int)tiles_s[t].size());
+        ps.insert(ps.end(), tiles_s[t].begin(), tiles_s[t].end());
+        plb.insert(plb.end(), tiles_lb[t].begin(), tiles_lb[t].end());
+    }
+    b.pad_ptr.upload(pptr);
+    b.pad_s.upload(ps);
+    b.pad_lb.upload(plb);
+    b.n_pad = (long long)ps.size();
+    p.use_bins = true;
+    p.tmap_ptr = nullptr;   // invalidate descriptor caches (box depends on T)
+}
+
+// --------------------------------------------------------------- TMA helpers --
+static PFN_cuTensorMapEncodeTiled_v12000 get_encode() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    if (!fn) {
+        cudaDriverEntryPointQueryResult q;
+        void* f = nullptr;
+        MMR_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q));
+        MMR_REQUIRE(q == cudaDriverEntryPointSuccess && f, "cuTensorMapEncodeTiled unavailable");
+        fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+    }
+    return fn;
+}
+
+// 3D map over a centered grid [G1, G2, nb] of complex64 viewed as floats.
+static void encode_grid_map(CUtensorMap* m, const void* grid, int G1, int G2, long long nb, int box_cells, int cg) {
+    MMR_REQUIRE(((uintptr_t)grid & 15) == 0, "grid buffer not 16-byte aligned");
+    cuuint64_t dims[3] = {(cuuint64_t)2 * G1, (cuuint64_t)G2, (cuuint64_t)nb};
+    cuuint64_t strides[2] = {(cuuint64_t)G1 * 8, (cuuint64_t)G1 * G2 * 8};
+    cuuint32_t box[3] = {(cuuint32_t)(2 * box_cells), (cuuint32_t)box_cells, (cuuint32_t)cg};
+    cuuint32_t es[3] = {1, 1, 1};
+    MMR_REQUIRE((2 * box_cells * 4) % 16 == 0 && 2 * box_cells <= 256 && box_cells <= 256 && cg <= 256,
+                "bad TMA box");
+    CUresult r = get_encode()(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void*>(grid), dims, strides, box,
+                              es, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                              CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    MMR_REQUIRE(r == CUDA_SUCCESS, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+// Bounded mbarrier wait: returns false (and flags the device error word) on timeout.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
+    const uint32_t a = smem_u32(bar);
+    for (int it = 0; it < (1 << 22); ++it) {
+        uint32_t done;
+        asm volatile(
+            "{\n\t.reg .pred p;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "selp.u32 %0, 1, 0, p;\n\t}\n"
+            : "=r"(done)
+            : "r"(a), "r"(phase)
+            : "memory");
+        if (done) return true;
+    }
+    atomicExch(&g_dev_error, 1);
+    return false;
+}
+
+// Stage a [cg][R][R] complex region whose origin is (ox, oy) into smem.
+// TMA when the region is inside the grid, wrapped plain loads otherwise.
+__device__ __forceinline__ bool stage_region(float2* reg, const float2* __restrict__ grid, const CUtensorMap* tmap,
+                                             bool use_tma, uint64_t* bar, int ox, int oy, int c0, int cg, int R,
+                                             int G1, int G2, long long nb) {
+    // TMA only for regions fully inside the grid whose inner start (2*ox floats) is
+    // 16-byte aligned and whose row (2*R floats) is a multiple of 16 bytes.
+    const bool inside = use_tma && ox >= 0 && oy >= 0 && ox + R <= G1 && oy + R <= G2 && (ox & 1) == 0 &&
+                        (R & 1) == 0;
+    if (inside) {
+        if (threadIdx.x == 0) {
+            const uint32_t bytes = (uint32_t)cg * R * R * 8;
+            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                         : "memory");
+            asm volatile(
+                "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+                "%4}], [%5];" ::"r"(smem_u32(reg)),
+                "l"(tmap), "r"(2 * ox), "r"(oy), "r"(c0), "r"(smem_u32(bar))
+                : "memory");
+        }
+        const bool ok = mbar_wait(bar, 0);
+        return ok;
+    }
+    const int n = cg * R * R;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int c = i / (R * R), r = i - c * R * R, ry = r / R, rx = r - ry * R;
+        int u1 = ox + rx, u2 = oy + ry;
+        u1 += (u1 < 0) ? G1 : 0;
+        u1 -= (u1 >= G1) ? G1 : 0;
+        u2 += (u2 < 0) ? G2 : 0;
+        u2 -= (u2 >= G2) ? G2 : 0;
+        float2 v = make_float2(0.f, 0.f);
+        if (c0 + c < nb) v = grid[u1 + (long long)G1 * (u2 + (long long)G2 * (c0 + c))];
+        reg[i] = v;
+    }
+    __syncthreads();
+    return true;
+}
+
+// Dynamic smem layout for TMA kernels: [pad to 128 B][mbarrier, 128 B slot][region ...].
+constexpr size_t kTmaSmemExtra = 256;
+__device__ __forceinline__ float2* tma_layout(float4* sm, uint64_t** bar) {
+    char* b = reinterpret_cast<char*>(sm);
+    const uint32_t pad = (128u - (smem_u32(b) & 127u)) & 127u;
+    *bar = reinterpret_cast<uint64_t*>(b + pad);
+    return reinterpret_cast<float2*>(b + pad + 128);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar) {
+    if (threadIdx.x == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+}
+
+template <int W>
+struct TapMap {
+    static constexpr int TAPS = W * W;
+    static constexpr int LPP = TAPS <= 16 ? 16 : 32;          // lanes per (sample, coil) pair
+    static constexpr int TPL = (TAPS + LPP - 1) / LPP;        // taps per lane
+    static constexpr int PPW = 32 / LPP;                      // pairs per warp
+};
+
+template <int LPP>
+__device__ __forceinline__ float2 group_sum(float2 v) {
+#pragma unroll
+    for (int o = LPP / 2; o >= 1; o >>= 1) {
+        v.x += __shfl_xor_sync(0xffffffffu, v.x, o);
+        v.y += __shfl_xor_sync(0xffffffffu, v.y, o);
+    }
+    return v;
+}
+
+// ------------------------------------------------------- binned 2D kernels ----
+struct Bin2DArgs {
+    const int* ptr;
+    const int* ent_s;
+    const short2* ent_lb;
+    const float* wts;        // [M][2][W]
+    const float* wfac;       // per-sample weight or null
+    long long wfac_bstride;  // 0 or M
+    int G1, G2, T, ntx;
+    long long M, nb;
+    int cg;
+    int use_tma;
+    const int* active;
+};
+
+template <int W>
+__global__ void __launch_bounds__(256) interp2d_binned(const float2* __restrict__ grid, float2* __restrict__ y,
+                                                       const Bin2DArgs a, const __grid_constant__ CUtensorMap tmap) {
+    using TM = TapMap<W>;
+    extern __shared__ float4 sm4[];
+    if (a.active && *a.active) return;
+    const int R = a.T + W;
+    uint64_t* bar;
+    float2* reg = tma_layout(sm4, &bar);
+    const int tile = blockIdx.x;
+    const int c0 = blockIdx.y * a.cg;
+    const int e0 = a.ptr[tile], e1 = a.ptr[tile + 1];
+    if (e0 == e1) return;
+    const int tx = tile % a.ntx, ty = tile / a.ntx;
+    mbar_init(bar);
+    if (!stage_region(reg, grid, &tmap, a.use_tma, bar, tx * a.T - W / 2, ty * a.T - W / 2, c0, a.cg, R, a.G1, a.G2,
+                      a.nb))
+        return;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    const int grp = lane / TM::LPP, gl = lane % TM::LPP;
+    const int npairs = (e1 - e0) * a.cg;
+    for (int pb = warp * TM::PPW; pb < npairs; pb += nwarp * TM::PPW) {
+        const int pi = pb + grp;
+        float2 acc = make_float2(0.f, 0.f);
+        int s = 0, c = 0;
+        const bool valid = pi < npairs;
+        if (valid) {
+            const int e = e0 + pi / a.cg;
+            c = pi % a.cg;
+            s = a.ent_s[e];
+            const short2 lb = a.ent_lb[e];
+            const float* w = a.wts + (size_t)s * 2 * W;
+            const float2* rc = reg + (size_t)c * R * R;
+#pragma unroll
+            for (int i = 0; i < TM::TPL; ++i) {
+                const int k = gl + i * TM::LPP;
+                if (k < TM::TAPS) {
+                    const int ta = k % W, tb = k / W;
+                    const float wt = w[ta] * w[W + tb];
+                    const float2 g = rc[(lb.y + tb + 1) * R + (lb.x + ta + 1)];
+                    acc.x += wt * g.x;
+                    acc.y += wt * g.y;
+                }
+            }
+        }
+        acc = group_sum<TM::LPP>(acc);
+        if (valid && gl == 0 && c0 + c < a.nb) {
+            float f = 1.f;
+            if (a.wfac) f = a.wfac[s + a.wfac_bstride * (c0 + c)];
+            y[s + a.M * (c0 + c)] = make_float2(acc.x * f, acc.y * f);
+        }
+    }
+}
+
+template <int W>
+__global__ void __launch_bounds__(256) spread2d_binned(const float2* __restrict__ y, float2* __restrict__ grid,
+                                                       const Bin2DArgs a) {
+    using TM = TapMap<W>;
+    extern __shared__ float4 sm4[];
+    if (a.active && *a.active) return;
+    float2* acc = reinterpret_cast<float2*>(sm4);
+    const int T = a.T;
+    const int tile = blockIdx.x;
+    const int c0 = blockIdx.y * a.cg;
+    const int tx = tile % a.ntx, ty = tile / a.ntx;
+    const int u0 = tx * T, v0 = ty * T;
+    const int te1 = min(T, a.G1 - u0), te2 = min(T, a.G2 - v0);
+    for (int i = threadIdx.x; i < a.cg * T * T; i += blockDim.x) acc[i] = make_float2(0.f, 0.f);
+    __syncthreads();
+    const int e0 = a.ptr[tile], e1 = a.ptr[tile + 1];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    const int grp = lane / TM::LPP, gl = lane % TM::LPP;
+    const int npairs = (e1 - e0) * a.cg;
+    constexpr int off0 = -W / 2 + 1;
+    for (int pb = warp * TM::PPW; pb < npairs; pb += nwarp * TM::PPW) {
+        const int pi = pb + grp;
+        if (pi >= npairs) continue;
+        const int e = e0 + pi / a.cg, c = pi % a.cg;
+        if (c0 + c >= a.nb) continue;
+        const int s = a.ent_s[e];
+        const short2 lb = a.ent_lb[e];
+        float2 v = y[s + a.M * (c0 + c)];
+        if (a.wfac) {
+            const float f = a.wfac[s + a.wfac_bstride * (c0 + c)];
+            v.x *= f;
+            v.y *= f;
+        }
+        const float* w = a.wts + (size_t)s * 2 * W;
+        float2* ac = acc + (size_t)c * T * T;
+#pragma unroll
+        for (int i = 0; i < TM::TPL; ++i) {
+            const int k = gl + i * TM::LPP;
+            if (k < TM::TAPS) {
+                const int ta = k % W, tb = k / W;
+                const int l1 = lb.x + off0 + ta, l2 = lb.y + off0 + tb;
+                if (l1 >= 0 && l1 < te1 && l2 >= 0 && l2 < te2) {
+                    const float wt = w[ta] * w[W + tb];
+                    atomicAdd(&ac[l2 * T + l1].x, wt * v.x);
+                    atomicAdd(&ac[l2 * T + l1].y, wt * v.y);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < a.cg * T * T; i += blockDim.x) {
+        const int c = i / (T * T), r = i - c * T * T, l2 = r / T, l1 = r - l2 * T;
+        if (l1 < te1 && l2 < te2 && c0 + c < a.nb)
+            grid[(u0 + l1) + (long long)a.G1 * ((v0 + l2) + (long long)a.G2 * (c0 + c))] = acc[i];
+    }
+}
+
+template <int W>
+__global__ void __launch_bounds__(256) gridnorm2d_binned(const float2* __restrict__ gin, float2* __restrict__ gout,
+                                                         const Bin2DArgs a, const __grid_constant__ CUtensorMap tmap) {
+    using TM = TapMap<W>;
+    extern __shared__ float4 sm4[];
+    if (a.active && *a.active) return;
+    const int T = a.T, R = T + 2 * W;
+    uint64_t* bar;
+    float2* reg = tma_layout(sm4, &bar);
+    float2* acc = reg + (size_t)a.cg * R * R;
+    const int tile = blockIdx.x;
+    const int c0 = blockIdx.y * a.cg;
+    const int tx = tile % a.ntx, ty = tile / a.ntx;
+    const int u0 = tx * T, v0 = ty * T;
+    const int te1 = min(T, a.G1 - u0), te2 = min(T, a.G2 - v0);
+    for (int i = threadIdx.x; i < a.cg * T * T; i += blockDim.x) acc[i] = make_float2(0.f, 0.f);
+    const int e0 = a.ptr[tile], e1 = a.ptr[tile + 1];
+    mbar_init(bar);
+    if (e1 > e0) {
+        if (!stage_region(reg, gin, &tmap, a.use_tma, bar, u0 - W, v0 - W, c0, a.cg, R, a.G1, a.G2, a.nb)) return;
+    }
+    __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    const int grp = lane / TM::LPP, gl = lane % TM::LPP;
+    const int npairs = (e1 - e0) * a.cg;
+    constexpr int off0 = -W / 2 + 1;
+    for (int pb = warp * TM::PPW; pb < npairs; pb += nwarp * TM::PPW) {
+        const int pi = pb + grp;
+        const bool valid = pi < npairs;
+        int e = e0, c = 0, s = 0;
+        short2 lb = make_short2(0, 0);
+        if (valid) {
+            e = e0 + pi / a.cg;
+            c = pi % a.cg;
+            s = a.ent_s[e];
+            lb = a.ent_lb[e];
+        }
+        const float* w = a.wts + (size_t)s * 2 * W;
+        const float2* rc = reg + (size_t)c * R * R;
+        float2 v = make_float2(0.f, 0.f);
+        float wt[TM::TPL];
+#pragma unroll
+        for (int i = 0; i < TM::TPL; ++i) {
+            const int k = gl + i * TM::LPP;
+            wt[i] = 0.f;
+            if (valid && k < TM::TAPS) {
+                const int ta = k % W, tb = k / W;
+                wt[i] = w[ta] * w[W + tb];
+                const float2 g = rc[(lb.y + off0 + tb + W) * R + (lb.x + off0 + ta + W)];
+                v.x += wt[i] * g.x;
+                v.y += wt[i] * g.y;
+            }
+        }
+        v = group_sum<TM::LPP>(v);
+        if (!valid || c0 + c >= a.nb) continue;
+        if (a.wfac) {
+            const float f = a.wfac[s + a.wfac_bstride * (c0 + c)];
+            v.x *= f;
+            v.y *= f;
+        }
+        float2* ac = acc + (size_t)c * T * T;
+#pragma unroll
+        for (int i = 0; i < TM::TPL; ++i) {
+            const int k = gl + i * TM::LPP;
+            if (k < TM::TAPS) {
+                const int ta = k % W, tb = k / W;
+                const int l1 = lb.x + off0 + ta, l2 = lb.y + off0 + tb;
+                if (l1 >= 0 && l1 < te1 && l2 >= 0 && l2 < te2) {
+                    atomicAdd(&ac[l2 * T + l1].x, wt[i] * v.x);
+                    atomicAdd(&ac[l2 * T + l1].y, wt[i] * v.y);
+                }
+            }
+        }
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < a.cg * T * T; i += blockDim.x) {
+        const int c = i / (T * T), r = i - c * T * T, l2 = r / T, l1 = r - l2 * T;
+        if (l1 < te1 && l2 < te2 && c0 + c < a.nb)
+            gout[(u0 + l1) + (long long)a.G1 * ((v0 + l2) + (long long)a.G2 * (c0 + c))] = acc[i];
+    }
+}
+
+// ------------------------------------------------------------ generic kernels --
+struct GenArgs {
+    const int* base;     // [nd][M]
+    const float* wts;    // [M][nd][W]
+    const float* wfac;
+    long long wfac_bstride;
+    int nd, W;
+    int G1, G2, G3;
+    long long M, nb;
+    const int* active;
+};
+
+__global__ void interp_generic(const float2* __restrict__ grid, float2* __restrict__ y, const GenArgs a) {
+    if (a.active && *a.active) return;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.M * a.nb) return;
+    const long long s = i % a.M, bb = i / a.M;
+    const int W = a.W, off0 = -W / 2 + 1;
+    const float* w = a.wts + (size_t)s * a.nd * W;
+    const int c1 = a.base[s];
+    const int c2 = a.nd > 1 ? a.base[a.M + s] : 0;
+    const int c3 = a.nd > 2 ? a.base[2 * a.M + s] : 0;
+    const long long Gt = (long long)a.G1 * a.G2 * a.G3;
+    const float2* g = grid + Gt * bb;
+    float2 acc = make_float2(0.f, 0.f);
+    const int n2 = a.nd > 1 ? W : 1, n3 = a.nd > 2 ? W : 1;
+    for (int k3 = 0; k3 < n3; ++k3) {
+        int u3 = 0;
+        float w3 = 1.f;
+        if (a.nd > 2) { u3 = c3 + off0 + k3; u3 += u3 < 0 ? a.G3 : 0; u3 -= u3 >= a.G3 ? a.G3 : 0; w3 = w[2 * W + k3]; }
+        for (int k2 = 0; k2 < n2; ++k2) {
+            int u2 = 0;
+            float w2 = 1.f;
+            if (a.nd > 1) { u2 = c2 + off0 + k2; u2 += u2 < 0 ? a.G2 : 0; u2 -= u2 >= a.G2 ? a.G2 : 0; w2 = w[W + k2]; }
+            for (int k1 = 0; k1 < W; ++k1) {
+                int u1 = c1 + off0 + k1;
+                u1 += u1 < 0 ? a.G1 : 0;
+                u1 -= u1 >= a.G1 ? a.G1 : 0;
+                const float wt = w[k1] * w2 * w3;
+                const float2 v = g[u1 + (long long)a.G1 * (u2 + (long long)a.G2 * u3)];
+                acc.x += wt * v.x;
+                acc.y += wt * v.y;
+            }
+        }
+    }
+    float f = 1.f;
+    if (a.wfac) f = a.wfac[s + a.wfac_bstride * bb];
+    y[i] = make_float2(acc.x * f, acc.y * f);
+}
+
+__global__ void spread_generic(const float2* __restrict__ y, float2* __restrict__ grid, const GenArgs a) {
+    if (a.active && *a.active) return;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.M * a.nb) return;
+    const long long s = i % a.M, bb = i / a.M;
+    const int W = a.W, off0 = -W / 2 + 1;
+    const float* w = a.wts + (size_t)s * a.nd * W;
+    float2 v = y[i];
+    if (a.wfac) {
+        const float f = a.wfac[s + a.wfac_bstride * bb];
+        v.x *= f;
+        v.y *= f;
+    }
+    const int c1 = a.base[s];
+    const int c2 = a.nd > 1 ? a.base[a.M + s] : 0;
+    const int c3 = a.nd > 2 ? a.base[2 * a.M + s] : 0;
+    const long long Gt = (long long)a.G1 * a.G2 * a.G3;
+    float2* g = grid + Gt * bb;
+    const int n2 = a.nd > 1 ? W : 1, n3 = a.nd > 2 ? W : 1;
+    for (int k3 = 0; k3 < n3; ++k3) {
+        int u3 = 0;
+        float w3 = 1.f;
+        if (a.nd > 2) { u3 = c3 + off0 + k3; u3 += u3 < 0 ? a.G3 : 0; u3 -= u3 >= a.G3 ? a.G3 : 0; w3 = w[2 * W + k3]; }
+        for (int k2 = 0; k2 < n2; ++k2) {
+            int u2 = 0;
+            float w2 = 1.f;
+            if (a.nd > 1) { u2 = c2 + off0 + k2; u2 += u2 < 0 ? a.G2 : 0; u2 -= u2 >= a.G2 ? a.G2 : 0; w2 = w[W + k2]; }
+            for (int k1 = 0; k1 < W; ++k1) {
+                int u1 = c1 + off0 + k1;
+                u1 += u1 < 0 ? a.G1 : 0;
+                u1 -= u1 >= a.G1 ? a.G1 : 0;
+                const float wt = w[k1] * w2 * w3;
+                float2* d = g + u1 + (long long)a.G1 * (u2 + (long long)a.G2 * u3);
+                atomicAdd(&d->x, wt * v.x);
+                atomicAdd(&d->y, wt * v.y);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------- dispatch ----
+static int pick_cg(const NufftPlan& p, long long nb, size_t per_coil_bytes, size_t fixed) {
+    const size_t lim = (size_t)std::min(device_smem_optin(), 200 * 1024);
+    int cg = 8;
+    while (cg > 1 && fixed + per_coil_bytes * cg > lim) cg /= 2;
+    while (cg > 1 && cg / 2 >= nb) cg /= 2;
+    return cg;
+}
+
+static Bin2DArgs bin_args(const NufftPlan& p, bool own, const float* wfac, long long wfb, long long nb, int cg,
+                          bool tma, const int* active) {
+    Bin2DArgs a;
+    const BinLists& b = p.bins;
+    a.ptr = own ? b.own_ptr.as<int>() : b.pad_ptr.as<int>();
+    a.ent_s = own ? b.own_s.as<int>() : b.pad_s.as<int>();
+    a.ent_lb = own ? b.own_lb.as<short2>() : b.pad_lb.as<short2>();
+    a.wts = p.d_w.as<float>();
+    a.wfac = wfac;
+    a.wfac_bstride = wfb;
+    a.G1 = p.G[0];
+    a.G2 = p.G[1];
+    a.T = b.T;
+    a.ntx = b.ntx;
+    a.M = p.M;
+    a.nb = nb;
+    a.cg = cg;
+    a.use_tma = tma ? 1 : 0;
+    a.active = active;
+    return a;
+}
+
+template <class K>
+static void set_smem(K kern, size_t smem) {
+    MMR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+}
+
+#define MMR_W_DISPATCH(W, ...)                                \
+    switch (W) {                                              \
+        case 2: { constexpr int KW = 2; __VA_ARGS__; } break; \
+        case 4: { constexpr int KW = 4; __VA_ARGS__; } break; \
+        case 6: { constexpr int KW = 6; __VA_ARGS__; } break; \
+        case 8: { constexpr int KW = 8; __VA_ARGS__; } break; \
+        default: MMR_THROW(MMR_ERR_UNSUPPORTED, "kwidth %d", (W)); \
+    }
+
+static GenArgs gen_args(const NufftPlan& p, const float* wfac, long long wfb, long long nb, const int* active) {
+    GenArgs g;
+    g.base = p.d_base.as<int>();
+    g.wts = p.d_w.as<float>();
+    g.wfac = wfac;
+    g.wfac_bstride = wfb;
+    g.nd = p.nd;
+    g.W = p.W;
+    g.G1 = p.G[0];
+    g.G2 = p.G[1];
+    g.G3 = p.G[2];
+    g.M = p.M;
+    g.nb = nb;
+    g.active = active;
+    return g;
+}
+
+void nufft_interp(NufftPlan& p, const float2* grid, float2* y, long long nb, const float* wfac, long long wfb,
+                  cudaStream_t st, const int* active) {
+    if (!p.use_bins) {
+        const long long n = p.M * nb;
+        interp_generic<<<(unsigned)cdiv(n, 256), 256, 0, st>>>(grid, y, gen_args(p, wfac, wfb, nb, active));
+        check_launch("interp_generic");
+        return;
+    }
+    const int R = p.bins.T + p.W;
+    const int cg = pick_cg(p, nb, (size_t)R * R * 8, kTmaSmemExtra);
+    if (p.tmap_ptr != grid || p.tmap_nb != nb || p.tmap_cg != cg) {
+        encode_grid_map(&p.tmap, grid, p.G[0], p.G[1], nb, R, cg);
+        p.tmap_ptr = grid;
+        p.tmap_nb = nb;
+        p.tmap_cg = cg;
+    }
+    const size_t smem = kTmaSmemExtra + (size_t)cg * R * R * 8;
+    Bin2DArgs a = bin_args(p, true, wfac, wfb, nb, cg, true, active);
+    dim3 gridDim((unsigned)(p.bins.ntx * p.bins.nty), (unsigned)cdiv(nb, cg));
+    MMR_W_DISPATCH(p.W, {
+        set_smem(interp2d_binned<KW>, smem);
+        interp2d_binned<KW><<<gridDim, 256, smem, st>>>(grid, y, a, p.tmap);
+    });
+    check_launch("interp2d_binned");
+}
+
+void nufft_spread(NufftPlan& p, const float2* y, float2* grid, long long nb, const float* wfac, long long wfb,
+                  cudaStream_t st, const int* active) {
+    if (!p.use_bins) {
+        MMR_CUDA(cudaMemsetAsync(grid, 0, (size_t)p.Gtot * nb * sizeof(float2), st));
+        const long long n = p.M * nb;
+        spread_generic<<<(unsigned)cdiv(n, 256), 256, 0, st>>>(y, grid, gen_args(p, wfac, wfb, nb, active));
+        check_launch("spread_generic");
+        return;
+    }
+    const int T = p.bins.T;
+    const int cg = pick_cg(p, nb, (size_t)T * T * 8, 0);
+    const size_t smem = (size_t)cg * T * T * 8;
+    Bin2DArgs a = bin_args(p, false, wfac, wfb, nb, cg, false, active);
+    dim3 gridDim((unsigned)(p.bins.ntx * p.bins.nty), (unsigned)cdiv(nb, cg));
+    MMR_W_DISPATCH(p.W, {
+        set_smem(spread2d_binned<KW>, smem);
+        spread2d_binned<KW><<<gridDim, 256, smem, st>>>(y, grid, a);
+    });
+    check_launch("spread2d_binned");
+}
+
+bool nufft_has_fused_normal(const NufftPlan& p) { return p.use_bins; }
+
+static CUtensorMap g_norm_map;   // cache for the fused kernel's box
+
+void nufft_grid_normal(NufftPlan& p, const float2* gin, float2* gout, long long nb, const float* wfac, long long wfb,
+                       cudaStream_t st, const int* active) {
+    MMR_REQUIRE(p.use_bins, "fused gridding needs the 2D binned path");
+    const int T = p.bins.T, R = T + 2 * p.W;
+    const int cg = pick_cg(p, nb, (size_t)(R * R + T * T) * 8, kTmaSmemExtra);
+    static const void* cptr = nullptr;
+    static long long cnb = 0;
+    static int ccg = 0, cR = 0, cG1 = 0, cG2 = 0;
+    if (cptr != gin || cnb != nb || ccg != cg || cR != R || cG1 != p.G[0] || cG2 != p.G[1]) {
+        encode_grid_map(&g_norm_map, gin, p.G[0], p.G[1], nb, R, cg);
+        cptr = gin;
+        cnb = nb;
+        ccg = cg;
+        cR = R;
+        cG1 = p.G[0];
+        cG2 = p.G[1];
+    }
+    const size_t smem = kTmaSmemExtra + (size_t)cg * (R * R + T * T) * 8;
+    Bin2DArgs a = bin_args(p, false, wfac, wfb, nb, cg, true, active);
+    dim3 gridDim((unsigned)(p.bins.ntx * p.bins.nty), (unsigned)cdiv(nb, cg));
+    MMR_W_DISPATCH(p.W, {
+        set_smem(gridnorm2d_binned<KW>, smem);
+        gridnorm2d_binned<KW><<<gridDim, 256, smem, st>>>(gin, gout, a, g_norm_map);
+    });
+    check_launch("gridnorm2d_binned");
+}
+
+// ------------------------------------------------------------- FFT pipelines --
+static PassArgs base_pass(const NufftPlan& p, int axis, int sign) {
+    PassArgs a;
+    a.L = p.G[axis];
+    a.f = p.ff[axis];
+    a.tw = p.tw[axis];
+    a.sign = sign;
+    a.scale = (float)(1.0 / std::sqrt((double)p.G[axis]));
+    a.B = std::max(1, std::min(16, 2048 / a.L));
+    return a;
+}
+
+void nufft_img_to_grid(NufftPlan& p, const float2* x, const float2* maps, float2* grid, long long nb, cudaStream_t st,
+                       const int* active) {
+    // axis order 0, 1, 2: image extents shrink to grid extents one axis at a time
+    long long ext[3] = {p.N[0], p.N[1], p.N[2]};
+    float2* tmp = nullptr;
+    if (p.nd > 1) {
+        // intermediate buffers: after axis 0: [G1, N2, N3, nb]; after axis 1: [G1, G2, N3, nb]
+        const size_t need = (size_t)p.G[0] * p.N[1] * p.N[2] * nb;
+        const size_t need2 = p.nd > 2 ? (size_t)p.G[0] * p.G[1] * p.N[2] * nb : 0;
+        p.s_tmp.ensure((need + need2) * sizeof(float2));
+        tmp = p.s_tmp.as<float2>();
+    }
+    const float2* src = x;
+    for (int ax = 0; ax < p.nd; ++ax) {
+        PassArgs a = base_pass(p, ax, +1);
+        long long inner = 1, outer = nb;
+        for (int k = 0; k < ax; ++k) inner *= p.G[k];
+        for (int k = ax + 1; k < 3; ++k) outer *= ext[k];
+        a.inner = inner;
+        a.outer = outer;
+        a.nin = p.N[ax];
+        a.in_start = p.G[ax] - p.N[ax] / 2;
+        a.nout = p.G[ax];
+        a.out_start = p.G[ax] / 2;
+        a.in_fac = p.d_fwd_fac[ax].as<float2>();
+        a.active = active;
+        float2* dst;
+        if (ax == p.nd - 1) dst = grid;
+        else if (ax == 0) dst = tmp;
+        else dst = tmp + (size_t)p.G[0] * p.N[1] * p.N[2] * nb;
+        a.in = src;
+        a.out = dst;
+        int mode = PASS_PLAIN;
+        if (ax == 0 && maps) {
+            mode = PASS_FWD_IMG;
+            a.maps = maps;
+            a.lpc = (long long)p.N[1] * p.N[2];
+        }
+        launch_fft_pass(mode, a, st);
+        ext[ax] = p.G[ax];
+        src = dst;
+    }
+}
+
+void nufft_grid_to_img(NufftPlan& p, const float2* grid, const float2* maps, float2* out, long long nb,
+                       bool accumulate, cudaStream_t st, const int* active) {
+    long long ext[3] = {p.G[0], p.G[1], p.G[2]};
+    float2* tmp = nullptr;
+    if (p.nd > 1) {
+        const size_t need = (size_t)p.N[0] * p.G[1] * p.G[2] * nb;
+        const size_t need2 = p.nd > 2 ? (size_t)p.N[0] * p.N[1] * p.G[2] * nb : 0;
+        p.s_tmp.ensure((need + need2) * sizeof(float2));
+        tmp = p.s_tmp.as<float2>();
+    }
+    const float2* src = grid;
+    for (int ax = 0; ax < p.nd; ++ax) {
+        PassArgs a = base_pass(p, ax, -1);
+        long long inner = 1, outer = nb;
+        for (int k = 0; k < ax; ++k) inner *= p.N[k];
+        for (int k = ax + 1; k < 3; ++k) outer *= ext[k];
+        a.inner = inner;
+        a.nin = p.G[ax];
+        a.in_start = p.G[ax] / 2;
+        a.nout = p.N[ax];
+        a.out_start = p.G[ax] - p.N[ax] / 2;
+        a.out_fac = p.d_adj_fac[ax].as<float2>();
+        a.active = active;
+        const bool last = ax == p.nd - 1;
+        float2* dst;
+        if (last) dst = out;
+        else if (ax == 0) dst = tmp;
+        else dst = tmp + (size_t)p.N[0] * p.G[1] * p.G[2] * nb;
+        a.in = src;
+        a.out = dst;
+        int mode = PASS_PLAIN;
+        if (last && maps) {
+            mode = PASS_ADJ_COMBINE;
+            a.maps = maps;
+            a.outer = nb;          // coils summed by the cluster
+            a.accumulate = accumulate ? 1 : 0;
+            a.B = std::max(1, std::min<int>(8, (int)std::min<long long>(inner, 2048 / a.L)));
+            if (inner == 1) a.B = 1;
+        } else {
+            a.outer = outer;
+        }
+        launch_fft_pass(mode, a, st);
+        ext[ax] = p.N[ax];
+        src = dst;
+    }
+}
+
+void nufft_forward(NufftPlan& p, const float2* x, float2* y, long long nb, cudaStream_t st, const int* active) {
+    p.s_grid.ensure((size_t)p.Gtot * nb * sizeof(float2));
+    float2* grid = p.s_grid.as<float2>();
+    nufft_img_to_grid(p, x, nullptr, grid, nb, st, active);
+    nufft_interp(p, grid, y, nb, p.has_dcf ? p.d_dcf.as<float>() : nullptr, 0, st, active);
+}
+
+void nufft_adjoint(NufftPlan& p, const float2* y, float2* x, long long nb, cudaStream_t st, const int* active) {
+    p.s_grid.ensure((size_t)p.Gtot * nb * sizeof(float2));
+    float2* grid = p.s_grid.as<float2>();
+    nufft_spread(p, y, grid, nb, p.has_dcf ? p.d_dcf.as<float>() : nullptr, 0, st, active);
+    nufft_grid_to_img(p, grid, nullptr, x, nb, false, st, active);
+}
+
+// ------------------------------------------------------------------ Toeplitz --
+__global__ void cmul_bcast_kernel(float2* __restrict__ x, const float2* __restrict__ t, long long n, long long nt) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] = cmul(x[i], t[i % nt]);
+}
+
+__global__ void cscale_kernel(float2* __restrict__ x, float s, long long n) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) x[i] = cscale(x[i], s);
+}
+
+// Centered (i)fft passes on a [2N]^d grid: ifftnc/fftnc with doShift = 1 (general/fftnc.m:32-42).
+static void toep_passes(NufftPlan& p, const float2* in, float2* out, long long nb, int sign, int nin_mode,
+                        cudaStream_t st, float2* tmp) {
+    // nin_mode 0: input is the N-image (pad to 2N, centered) -> output full 2N grid
+    // nin_mode 1: input is the full 2N grid -> output cropped N-image
+    // nin_mode 2: full 2N grid -> full 2N grid
+    long long ext[3];
+    int L[3] = {1, 1, 1};
+    for (int k = 0; k < 3; ++k) {
+        L[k] = k < p.nd ? 2 * p.N[k] : 1;
+        ext[k] = (nin_mode == 0) ? (k < p.nd ? p.N[k] : 1) : L[k];
+    }
+    const float2* src = in;
+    for (int ax = 0; ax < p.nd; ++ax) {
+        PassArgs a;
+        a.L = L[ax];
+        a.f = p.tff[ax];
+        a.tw = p.ttw[ax];
+        a.sign = sign;
+        a.scale = (float)(1.0 / std::sqrt((double)L[ax]));
+        a.B = std::max(1, std::min(16, 2048 / a.L));
+        long long inner = 1, outer = nb;
+        int outn = (nin_mode == 1) ? p.N[ax] : L[ax];
+        for (int k = 0; k < ax; ++k) inner *= (nin_mode == 1 ? p.N[k] : L[k]);
+        for (int k = ax + 1; k < 3; ++k) outer *= ext[k];
+        a.inner = inner;
+        a.outer = outer;
+        if (nin_mode == 0) { a.nin = p.N[ax]; a.in_start = L[ax] - p.N[ax] / 2; }
+        else { a.nin = L[ax]; a.in_start = L[ax] / 2; }
+        a.nout = outn;
+        a.out_start = (nin_mode == 1) ? L[ax] - p.N[ax] / 2 : L[ax] / 2;
+        const bool last = ax == p.nd - 1;
+        float2* dst = last ? out : tmp + (size_t)(ax & 1) * (size_t)(8LL * p.Ntot * nb);
+        a.in = src;
+        a.out = dst;
+        launch_fft_pass(PASS_PLAIN, a, st);
+        ext[ax] = outn;
+        src = dst;
+    }
+}
+
+void nufft_prep_toep(NufftPlan& p, double tos, int kw) {
+    if (p.is_toep) return;
+    if (tos <= 0) tos = 0.5 * (p.os - 1) + 1;                               // nufftOp.m:416
+    if (kw <= 0) kw = p.W;
+    mmr_nufft_desc d = {};
+    d.ndim = p.nd;
+    for (int k = 0; k < p.nd; ++k) d.imN[k] = 2 * p.N[k];
+    d.nsamp = p.M;
+    d.kloc = p.kloc.data();
+    d.dcf = p.dcf_h.empty() ? nullptr : p.dcf_h.data();
+    d.os = tos;
+    d.kwidth = kw;
+    NufftPlan S;
+    nufft_plan_build(S, d);                                                 // nufftOp.m:421
+    std::vector<float2> v(p.M);
+    for (long long s = 0; s < p.M; ++s) v[s] = make_float2(p.dcf_h.empty() ? 1.f : (float)p.dcf_h[s], 0.f);
+    DevBuf dv, dimg;
+    dv.upload(v);
+    long long n2 = 1;
+    for (int k = 0; k < p.nd; ++k) {
+        n2 *= 2 * p.N[k];
+        p.tff[k] = fft_factorize(2 * p.N[k]);
+        p.ttw[k] = fft_twiddles(2 * p.N[k]);
+    }
+    dimg.ensure(n2 * sizeof(float2));
+    nufft_adjoint(S, dv.as<float2>(), dimg.as<float2>(), 1, 0, nullptr);   // S'*dcf (423/425)
+    p.d_toep.ensure(n2 * sizeof(float2));
+    DevBuf tmp;
+    tmp.ensure((size_t)2 * 8 * p.Ntot * sizeof(float2));
+    toep_passes(p, dimg.as<float2>(), p.d_toep.as<float2>(), 1, +1, 2, 0, tmp.as<float2>());  // ifftnc (427)
+    cscale_kernel<<<(unsigned)cdiv(n2, 256), 256>>>(p.d_toep.as<float2>(), (float)(1 << p.nd), n2);
+    check_launch("cscale");
+    MMR_CUDA(cudaDeviceSynchronize());
+    p.is_toep = true;
+}
+
+void nufft_toep_apply(NufftPlan& p, const float2* x, float2* y, long long nb, cudaStream_t st) {
+    long long n2 = 1;
+    for (int k = 0; k < p.nd; ++k) n2 *= 2 * p.N[k];
+    p.s_grid.ensure((size_t)n2 * nb * sizeof(float2));
+    p.s_grid2.ensure((size_t)2 * 8 * p.Ntot * nb * sizeof(float2));
+    float2* g = p.s_grid.as<float2>();
+    toep_passes(p, x, g, nb, +1, 0, st, p.s_grid2.as<float2>());           // ifftnc(padcrop(x, 2N))
+    cmul_bcast_kernel<<<(unsigned)cdiv(n2 * nb, 256), 256, 0, st>>>(g, p.d_toep.as<float2>(), n2 * nb, n2);
+    check_launch("toep multiply");
+    toep_passes(p, g, y, nb, -1, 1, st, p.s_grid2.as<float2>());           // padcrop(fftnc(.), N)
+}
+
+}  // namespace mmr

@@ -1,0 +1,93 @@
+// @nufftOp plan and gridding kernels (Kaiser-Bessel interpolation / spreading).
+#pragma once
+
+#include <cuda.h>
+
+#include "fft.cuh"
+
+namespace mmr {
+
+// Binned sample lists for one tile size (2D fast path).
+struct BinLists {
+    int T = 0;                 // tile side (grid cells)
+    int ntx = 0, nty = 0;
+    DevBuf own_ptr, own_s, own_lb;   // interp: each sample once (tile containing its base cell)
+    DevBuf pad_ptr, pad_s, pad_lb;   // spread/normal: every tile its footprint touches
+    long long n_own = 0, n_pad = 0;
+    int max_own = 0, max_pad = 0;
+};
+
+struct NufftPlan {
+    int nd = 0;
+    int N[3] = {1, 1, 1};
+    int G[3] = {1, 1, 1};
+    long long M = 0;
+    int W = 0;
+    double os = 0, beta = 0;
+    int Nkern = 0;
+    long long Ntot = 1, Gtot = 1;
+    std::vector<double> kloc;     // host copy [M x nd] (Toeplitz re-plans from it)
+    std::vector<double> dcf_h;    // host copy (empty = no dcf)
+    DevBuf d_base;                // int  [nd][M]: floor((k+0.5) G) mod G
+    DevBuf d_w;                   // float [M][nd][W] tap weights
+    DevBuf d_dcf;                 // float [M]
+    bool has_dcf = false;
+    int dcf_version = 0;
+    DevBuf d_fwd_fac[3], d_adj_fac[3];   // float2 [N_d]: deapod * exp(+-i pi N_d / 2)
+    FftFactors ff[3];
+    const float2* tw[3] = {nullptr, nullptr, nullptr};
+    BinLists bins;                // valid when use_bins
+    bool use_bins = false;
+    // scratch
+    DevBuf s_tmp, s_grid, s_grid2;
+    Staged st_in, st_out;
+    // TMA descriptor cache for the interp kernel (keyed by grid buffer / batch)
+    CUtensorMap tmap;
+    const void* tmap_ptr = nullptr;
+    long long tmap_nb = 0;
+    int tmap_cg = 0;
+    // Toeplitz mode
+    bool is_toep = false;
+    DevBuf d_toep;                // complex64 [2N...] transfer function (centered)
+    FftFactors tff[3];
+    const float2* ttw[3] = {nullptr, nullptr, nullptr};
+};
+
+void nufft_plan_build(NufftPlan& p, const mmr_nufft_desc& d);
+void nufft_set_dcf(NufftPlan& p, const double* dcf);
+void nufft_build_bins(NufftPlan& p, int T);
+
+// Operations on device buffers (all on `st`).  `active` (nullable) makes every
+// kernel a no-op while *active != 0 (device-resident solver termination).
+// x: [N..., nb]   grid: [G..., nb] centered   y: [M, nb]
+void nufft_forward(NufftPlan& p, const float2* x, float2* y, long long nb, cudaStream_t st,
+                   const int* active = nullptr);
+void nufft_adjoint(NufftPlan& p, const float2* y, float2* x, long long nb, cudaStream_t st,
+                   const int* active = nullptr);
+void nufft_toep_apply(NufftPlan& p, const float2* x, float2* y, long long nb, cudaStream_t st);
+void nufft_prep_toep(NufftPlan& p, double tos, int kw);
+
+// Building blocks used by the SENSE pipeline.
+// Image-domain -> centered oversampled grid for `nb` lines-sets.  When maps != null
+// the input is one image shared by the nb coils and multiplied by maps[.., c].
+void nufft_img_to_grid(NufftPlan& p, const float2* x, const float2* maps, float2* grid,
+                       long long nb, cudaStream_t st, const int* active);
+// Centered grid -> image (crop + deapod).  When maps != null, conj(maps) weighted sum
+// over the nb coils into out (accumulate: out += ...).
+void nufft_grid_to_img(NufftPlan& p, const float2* grid, const float2* maps, float2* out,
+                       long long nb, bool accumulate, cudaStream_t st, const int* active);
+// Gridding: interpolation (grid -> samples, times wfac) and spreading (samples*wfac -> grid).
+// wfac: per-sample real weight [M] or per-sample-per-batch [M x nb] (wfac_bstride = M), or null.
+void nufft_interp(NufftPlan& p, const float2* grid, float2* y, long long nb, const float* wfac,
+                  long long wfac_bstride, cudaStream_t st, const int* active);
+void nufft_spread(NufftPlan& p, const float2* y, float2* grid, long long nb, const float* wfac,
+                  long long wfac_bstride, cudaStream_t st, const int* active);
+// Fused C^H diag(wfac) C on the grid (interp -> weight -> spread), 2D binned path.
+void nufft_grid_normal(NufftPlan& p, const float2* gin, float2* gout, long long nb, const float* wfac,
+                       long long wfac_bstride, cudaStream_t st, const int* active);
+bool nufft_has_fused_normal(const NufftPlan& p);
+
+// Device error word set by bounded waits that ran out (0 = none).
+int device_error_word(cudaStream_t st);
+
+}  // namespace mmr

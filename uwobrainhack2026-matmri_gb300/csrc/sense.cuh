@@ -1,0 +1,69 @@
+// @rcvrOp, @sampHighOrder handle types and the mrSampFunc composition.
+#pragma once
+
+#include "nufft.cuh"
+
+namespace mmr {
+
+struct RcvrPlan {
+    int nd = 0;
+    int N[3] = {1, 1, 1};
+    long long Ntot = 0, C = 0;
+    DevBuf d_maps;   // complex64 [Ntot, C]
+    Staged st_in, st_out;
+};
+
+struct ShoPlan;   // sho.cuh
+
+// Forward / adjoint of sampHighOrder on device buffers (nb = batch columns).
+void sho_forward(ShoPlan& s, const float2* x, float2* y, long long nb, cudaStream_t st, const int* active);
+void sho_adjoint(ShoPlan& s, const float2* y, float2* x, long long nb, cudaStream_t st, const int* active);
+long long sho_nvox(const ShoPlan& s);
+long long sho_nsamp(const ShoPlan& s);
+
+void rcvr_forward(const RcvrPlan& r, const float2* x, float2* y, cudaStream_t st, const int* active);
+void rcvr_adjoint(const RcvrPlan& r, const float2* y, float2* x, cudaStream_t st, const int* active);
+
+// mrSampFunc(x, transp, S, R, opt) on device buffers.
+struct SenseOp {
+    NufftPlan* nufft = nullptr;
+    ShoPlan* sho = nullptr;
+    RcvrPlan* rcvr = nullptr;
+    long long Nimg = 0;     // voxels
+    long long M = 0;        // samples per coil
+    long long C = 1;        // coils (1 without R)
+    double tikreg = 0;
+    // opt.W (data weights, applied before the adjoint): [M] or [M x C]
+    DevBuf d_optW;
+    bool has_optW = false;
+    bool optW_per_coil = false;
+    int coil_chunk = 0;     // 0 = auto
+    int tile = 32;
+    // per-call weight buffers: dcf*W (adjoint) and dcf^2*W (normal)
+    DevBuf d_wadj, d_wnorm;
+    long long w_bstride = 0;
+    long long wkey = -2;    // cache key of d_wadj/d_wnorm when no cgne W is applied
+    std::vector<float> optW_h;
+    // scratch
+    DevBuf s_grid, s_grid2, s_samp, s_img;
+    Staged st_in, st_out;
+    cudaStream_t stream = nullptr;       // internal non-blocking stream (graphs)
+    void* solver_ws = nullptr;           // cg workspace (cg.cu)
+};
+
+int sense_chunk(const SenseOp& a);
+// Rebuilds d_wadj / d_wnorm from dcf, opt.W and an optional cgne W (host floats).
+void sense_set_weights(SenseOp& a, const float* cgW, bool cgW_per_coil);
+void sense_forward(SenseOp& a, const float2* x, float2* y, cudaStream_t st, const int* active);
+// adjoint applies d_wadj (dcf * opt.W * cgW)
+void sense_adjoint(SenseOp& a, const float2* y, float2* x, cudaStream_t st, const int* active);
+// normal op A^H diag(d_wnorm) A (+ tikreg^2) x
+void sense_normal(SenseOp& a, const float2* x, float2* y, cudaStream_t st, const int* active);
+
+void cg_release(SenseOp& a);
+
+}  // namespace mmr
+
+struct mmr_nufft { mmr::NufftPlan p; };
+struct mmr_rcvr { mmr::RcvrPlan r; };
+struct mmr_sense { mmr::SenseOp a; };

@@ -1,0 +1,340 @@
+// @sampHighOrder direct encoding on GB300.
+//
+// Phase (sampHighOrder.m:496-588, prepForDirect):
+//   kbase[v, m] = sum_n SH_n(r_v) phs_spha[n, m]      (b0mask on n > 4, 564-566)
+//               + sum_n conc_n(r_v) phs_conc[n, m]    (b0mask, 570-579)
+//               + b0[v] b0mask[v] t[m]                (580-586)
+// i.e. a real rank-K product B[V x K] P[K x M].  The plan forms B and P in
+// FP64 (basisFuncHarm.m:24-96, basisFuncConc.m:13-23), evaluates kbase once
+// on the device in FP64 and stores it reduced modulo 2*pi as FP32 "turns" in
+// [-1/2, 1/2) (absolute phase error ~2e-7 rad even where |kbase| ~ 1e3 rad).
+// Forward  y = exp(+i kbase.') x / sqrt(V)  (sampHighOrder.m:376, 387)
+// adjoint  x = exp(-i kbase)   y / sqrt(V)  (sampHighOrder.m:371, 387)
+// evaluate sincospi of the stored turns and accumulate in FP32.  Without room
+// for the table the kernels evaluate kbase per element in FP64 (the
+// no-precompute segmented approach 3, sampHighOrder.m:413-431).
+#include <algorithm>
+#include <cmath>
+
+#include "sense.cuh"
+
+namespace mmr {
+
+struct ShoPlan {
+    int nd = 0;
+    long long imN[3] = {1, 1, 1};
+    long long V = 0, M = 0;
+    int K = 0;
+    DevBuf d_B;     // double [K][V]
+    DevBuf d_P;     // double [K][M]
+    DevBuf d_turn;  // float  [V][M] (empty: on-the-fly FP64 phase)
+    bool table = false;
+    Staged st_in, st_out;
+};
+
+long long sho_nvox(const ShoPlan& s) { return s.V; }
+long long sho_nsamp(const ShoPlan& s) { return s.M; }
+
+static double harm(int n, double x, double y, double z) {
+    const double r2 = x * x + y * y + z * z;
+    switch (n) {
+        case 1: return 1.0;
+        case 2: return x;
+        case 3: return y;
+        case 4: return z;
+        case 5: return x * y;
+        case 6: return z * y;
+        case 7: return 3 * z * z - r2;
+        case 8: return x * z;
+        case 9: return x * x - y * y;
+        case 10: return 3 * y * x * x - y * y * y;
+        case 11: return x * z * y;
+        case 12: return (5 * z * z - r2) * y;
+        case 13: return 5 * z * z * z - 3 * z * r2;
+        case 14: return (5 * z * z - r2) * x;
+        case 15: return x * x * z - y * y * z;
+        case 16: return x * x * x - 3 * x * y * y;
+        case 17: return (x * y) * (x * x - y * y);
+        case 18: return (y * z) * (3 * x * x - y * y);
+        case 19: return (x * y) * (7 * z * z - r2);
+        case 20: return y * (7 * z * z * z - 3 * z * r2);
+        case 21: return 35 * z * z * z * z - 30 * z * z * r2 + 3 * r2 * r2;
+        case 22: return x * (7 * z * z * z - 3 * z * r2);
+        case 23: return (x * x - y * y) * (7 * z * z - r2);
+        case 24: return x * (x * x - 3 * y * y) * z;
+        case 25: return x * x * (x * x - 3 * y * y) - y * y * (3 * x * x - y * y);
+        case 26: return y * (5 * x * x * x * x - 10 * x * x * y * y + y * y * y * y);
+        case 27: return x * y * z * (x * x - y * y);
+        case 28: return y * (r2 - 9 * z * z) * (y * y - 3 * x * x);
+        case 29: return x * y * z * (3 * z * z - r2);
+        case 30: return y * (r2 * r2 - 14 * r2 * z * z + 21 * z * z * z * z);
+        case 31: return 63 * z * z * z * z * z - 70 * z * z * z * r2 + 15 * z * r2 * r2;
+        case 32: return x * (r2 * r2 - 14 * r2 * z * z + 21 * z * z * z * z);
+        case 33: return z * (3 * z * z - r2) * (x * x - y * y);
+        case 34: return x * (r2 - 9 * z * z) * (3 * y * y - x * x);
+        case 35: return z * (x * x * x * x - 6 * x * x * y * y + y * y * y * y);
+        case 36: return x * x * x * x * x - 10 * x * x * x * y * y + 5 * x * y * y * y * y;
+        default: return 0.0;
+    }
+}
+
+static double conc(int n, double x, double y, double z) {
+    switch (n) {
+        case 1: return z * z;
+        case 2: return x * x + y * y;
+        case 3: return x * z;
+        case 4: return y * z;
+        default: return 0.0;
+    }
+}
+
+__device__ __forceinline__ double sho_phase(const double* __restrict__ B, const double* __restrict__ P, int K,
+                                            long long V, long long M, long long v, long long m) {
+    double ph = 0.0;
+    for (int k = 0; k < K; ++k) ph = fma(B[k * V + v], P[k * M + m], ph);
+    return ph;
+}
+
+__device__ __forceinline__ float phase_turn(double ph) {
+    double t = ph * 0.15915494309189533577;   // 1 / (2 pi)
+    t -= rint(t);
+    return (float)t;
+}
+
+__global__ void sho_table_kernel(const double* __restrict__ B, const double* __restrict__ P, int K, long long V,
+                                 long long M, float* __restrict__ turn) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= V * M) return;
+    const long long v = i / M, m = i - v * M;
+    turn[i] = phase_turn(sho_phase(B, P, K, V, M, v, m));
+}
+
+// Forward: thread per sample m, CPT coils per thread, loop over voxels.
+template <int CPT>
+__global__ void __launch_bounds__(256) sho_fwd_kernel(const float* __restrict__ turn, const double* __restrict__ B,
+                                                      const double* __restrict__ P, int K, long long V, long long M,
+                                                      const float2* __restrict__ x, float2* __restrict__ y,
+                                                      long long nb, float scale, const int* active) {
+    if (active && *active) return;
+    constexpr int VC = 32;
+    __shared__ float2 xs[VC][CPT];
+    const long long m = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    const int c0 = blockIdx.y * CPT;
+    float2 acc[CPT];
+#pragma unroll
+    for (int c = 0; c < CPT; ++c) acc[c] = make_float2(0.f, 0.f);
+    for (long long v0 = 0; v0 < V; v0 += VC) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < VC * CPT; i += blockDim.x) {
+            const int vv = i / CPT, c = i - vv * CPT;
+            const long long v = v0 + vv;
+            xs[vv][c] = (v < V && c0 + c < nb) ? x[v + V * (c0 + c)] : make_float2(0.f, 0.f);
+        }
+        __syncthreads();
+        if (m < M) {
+            const int nv = (int)(V - v0 < VC ? V - v0 : VC);
+            for (int vv = 0; vv < nv; ++vv) {
+                const float t = turn ? turn[(v0 + vv) * M + m] : phase_turn(sho_phase(B, P, K, V, M, v0 + vv, m));
+                float s, c;
+                sincospif(2.f * t, &s, &c);
+#pragma unroll
+                for (int q = 0; q < CPT; ++q) {
+                    const float2 xv = xs[vv][q];
+                    acc[q].x += c * xv.x - s * xv.y;
+                    acc[q].y += c * xv.y + s * xv.x;
+                }
+            }
+        }
+    }
+    if (m < M) {
+#pragma unroll
+        for (int q = 0; q < CPT; ++q)
+            if (c0 + q < nb) y[m + M * (c0 + q)] = make_float2(acc[q].x * scale, acc[q].y * scale);
+    }
+}
+
+// Adjoint: thread per voxel v; the [256 v x 32 m] phase tile is staged through smem
+// so that the table is read along m (coalesced).
+template <int CPT>
+__global__ void __launch_bounds__(256) sho_adj_kernel(const float* __restrict__ turn, const double* __restrict__ B,
+                                                      const double* __restrict__ P, int K, long long V, long long M,
+                                                      const float2* __restrict__ y, float2* __restrict__ x,
+                                                      long long nb, float scale, const int* active) {
+    if (active && *active) return;
+    constexpr int MC = 32, VT = 256;
+    __shared__ float tt[VT][MC + 1];
+    __shared__ float2 ys[MC][CPT];
+    const long long v0 = (long long)blockIdx.x * VT;
+    const long long v = v0 + threadIdx.x;
+    const int c0 = blockIdx.y * CPT;
+    float2 acc[CPT];
+#pragma unroll
+    for (int c = 0; c < CPT; ++c) acc[c] = make_float2(0.f, 0.f);
+    for (long long m0 = 0; m0 < M; m0 += MC) {
+        __syncthreads();
+        for (int i = threadIdx.x; i < VT * MC; i += blockDim.x) {
+            const int vv = i / MC, mm = i - vv * MC;
+            const long long vg = v0 + vv, mg = m0 + mm;
+            float t = 0.f;
+            if (vg < V && mg < M) t = turn ? turn[vg * M + mg] : phase_turn(sho_phase(B, P, K, V, M, vg, mg));
+            tt[vv][mm] = t;
+        }
+        for (int i = threadIdx.x; i < MC * CPT; i += blockDim.x) {
+            const int mm = i / CPT, c = i - mm * CPT;
+            const long long mg = m0 + mm;
+            ys[mm][c] = (mg < M && c0 + c < nb) ? y[mg + M * (c0 + c)] : make_float2(0.f, 0.f);
+        }
+        __syncthreads();
+        if (v < V) {
+            const int nm = (int)(M - m0 < MC ? M - m0 : MC);
+            for (int mm = 0; mm < nm; ++mm) {
+                float s, c;
+                sincospif(2.f * tt[threadIdx.x][mm], &s, &c);
+#pragma unroll
+                for (int q = 0; q < CPT; ++q) {
+                    const float2 yv = ys[mm][q];
+                    acc[q].x += c * yv.x + s * yv.y;
+                    acc[q].y += c * yv.y - s * yv.x;
+                }
+            }
+        }
+    }
+    if (v < V) {
+#pragma unroll
+        for (int q = 0; q < CPT; ++q)
+            if (c0 + q < nb) x[v + V * (c0 + q)] = make_float2(acc[q].x * scale, acc[q].y * scale);
+    }
+}
+
+void sho_forward(ShoPlan& s, const float2* x, float2* y, long long nb, cudaStream_t st, const int* active) {
+    const float scale = (float)(1.0 / std::sqrt((double)s.V));
+    const float* tb = s.table ? s.d_turn.as<float>() : nullptr;
+    const unsigned gx = (unsigned)cdiv(s.M, 256);
+    if (nb > 4) {
+        sho_fwd_kernel<16><<<dim3(gx, (unsigned)cdiv(nb, 16)), 256, 0, st>>>(
+            tb, s.d_B.as<double>(), s.d_P.as<double>(), s.K, s.V, s.M, x, y, nb, scale, active);
+    } else if (nb > 1) {
+        sho_fwd_kernel<4><<<dim3(gx, (unsigned)cdiv(nb, 4)), 256, 0, st>>>(
+            tb, s.d_B.as<double>(), s.d_P.as<double>(), s.K, s.V, s.M, x, y, nb, scale, active);
+    } else {
+        sho_fwd_kernel<1><<<dim3(gx, 1), 256, 0, st>>>(tb, s.d_B.as<double>(), s.d_P.as<double>(), s.K, s.V, s.M, x,
+                                                       y, nb, scale, active);
+    }
+    check_launch("sho_fwd");
+}
+
+void sho_adjoint(ShoPlan& s, const float2* y, float2* x, long long nb, cudaStream_t st, const int* active) {
+    const float scale = (float)(1.0 / std::sqrt((double)s.V));
+    const float* tb = s.table ? s.d_turn.as<float>() : nullptr;
+    const unsigned gx = (unsigned)cdiv(s.V, 256);
+    if (nb > 4) {
+        sho_adj_kernel<16><<<dim3(gx, (unsigned)cdiv(nb, 16)), 256, 0, st>>>(
+            tb, s.d_B.as<double>(), s.d_P.as<double>(), s.K, s.V, s.M, y, x, nb, scale, active);
+    } else if (nb > 1) {
+        sho_adj_kernel<4><<<dim3(gx, (unsigned)cdiv(nb, 4)), 256, 0, st>>>(
+            tb, s.d_B.as<double>(), s.d_P.as<double>(), s.K, s.V, s.M, y, x, nb, scale, active);
+    } else {
+        sho_adj_kernel<1><<<dim3(gx, 1), 256, 0, st>>>(tb, s.d_B.as<double>(), s.d_P.as<double>(), s.K, s.V, s.M, y,
+                                                       x, nb, scale, active);
+    }
+    check_launch("sho_adj");
+}
+
+static void sho_build(ShoPlan& s, const mmr_sho_desc& d) {
+    MMR_REQUIRE(d.ndim >= 1 && d.ndim <= 3, "ndim must be 1..3");
+    MMR_REQUIRE(d.nsamp >= 1 && d.t && d.spha && d.gx && d.gy && d.gz, "missing sampHighOrder input");
+    MMR_REQUIRE(d.nspha >= 0 && d.nspha <= 36 && d.nconc >= 0 && d.nconc <= 4, "nspha <= 36, nconc <= 4");
+    MMR_REQUIRE(d.nconc == 0 || d.conc, "conc is NULL");
+    s.nd = d.ndim;
+    s.V = 1;
+    for (int k = 0; k < d.ndim; ++k) {
+        MMR_REQUIRE(d.imN[k] >= 1, "bad image size");
+        s.imN[k] = d.imN[k];
+        s.V *= d.imN[k];
+    }
+    s.M = d.nsamp;
+    const bool with_b0 = s.M > 1;                                          // 580
+    s.K = d.nspha + d.nconc + (with_b0 ? 1 : 0);
+    MMR_REQUIRE(s.K >= 1, "no phase terms");
+    std::vector<double> B((size_t)s.K * s.V), P((size_t)s.K * s.M);
+    int k = 0;
+    for (int n = 1; n <= d.nspha; ++n, ++k) {                              // 560-569
+        for (long long v = 0; v < s.V; ++v) {
+            double b = harm(n, d.gx[v], d.gy[v], d.gz[v]);
+            if (n > 4 && d.mask) b *= d.mask[v];
+            B[(size_t)k * s.V + v] = b;
+        }
+        for (long long m = 0; m < s.M; ++m) P[(size_t)k * s.M + m] = d.spha[(n - 1) + (size_t)d.nspha * m];
+    }
+    for (int n = 1; n <= d.nconc; ++n, ++k) {                              // 570-579
+        for (long long v = 0; v < s.V; ++v) {
+            double b = conc(n, d.gx[v], d.gy[v], d.gz[v]);
+            if (d.mask) b *= d.mask[v];
+            B[(size_t)k * s.V + v] = b;
+        }
+        for (long long m = 0; m < s.M; ++m) P[(size_t)k * s.M + m] = d.conc[(n - 1) + (size_t)d.nconc * m];
+    }
+    if (with_b0) {                                                          // 580-586
+        for (long long v = 0; v < s.V; ++v) {
+            double b = d.b0 ? d.b0[v] : 0.0;
+            if (d.mask) b *= d.mask[v];
+            B[(size_t)k * s.V + v] = b;
+        }
+        for (long long m = 0; m < s.M; ++m) P[(size_t)k * s.M + m] = d.t[m];
+        ++k;
+    }
+    for (double v : B) MMR_REQUIRE(std::isfinite(v), "non-finite basis value (check grid / b0 / mask)");
+    for (double v : P) MMR_REQUIRE(std::isfinite(v), "non-finite phase coefficient");
+    s.d_B.upload(B);
+    s.d_P.upload(P);
+    // Phase table: up to 8 GiB, and at most a quarter of the free memory.
+    size_t fr = 0, tot = 0;
+    MMR_CUDA(cudaMemGetInfo(&fr, &tot));
+    const size_t bytes = (size_t)s.V * s.M * sizeof(float);
+    s.table = bytes <= (8ull << 30) && bytes <= fr / 4;
+    if (s.table) {
+        s.d_turn.ensure(bytes);
+        const long long n = s.V * s.M;
+        sho_table_kernel<<<(unsigned)cdiv(n, 256), 256>>>(s.d_B.as<double>(), s.d_P.as<double>(), s.K, s.V, s.M,
+                                                          s.d_turn.as<float>());
+        check_launch("sho_table");
+        MMR_CUDA(cudaDeviceSynchronize());
+    }
+}
+
+}  // namespace mmr
+
+using namespace mmr;
+
+extern "C" int mmr_sho_create(const mmr_sho_desc* desc, mmr_sho** out) {
+    return guarded([&] {
+        MMR_REQUIRE(desc && out, "NULL argument");
+        *out = nullptr;
+        auto* s = new ShoPlan();
+        try {
+            sho_build(*s, *desc);
+        } catch (...) {
+            delete s;
+            throw;
+        }
+        *out = reinterpret_cast<mmr_sho*>(s);
+    });
+}
+
+extern "C" int mmr_sho_apply(mmr_sho* h, int adjoint, const void* in, void* out, int64_t nbatch, void* stream) {
+    return guarded([&] {
+        MMR_REQUIRE(h && in && out && nbatch >= 1, "bad argument");
+        ShoPlan& s = *reinterpret_cast<ShoPlan*>(h);
+        cudaStream_t st = as_stream(stream);
+        const size_t bv = (size_t)s.V * nbatch * 8, bm = (size_t)s.M * nbatch * 8;
+        const float2* din = (const float2*)stage_in(s.st_in, in, adjoint ? bm : bv, st);
+        float2* dout = (float2*)stage_out(s.st_out, out, adjoint ? bv : bm);
+        if (adjoint) sho_adjoint(s, din, dout, nbatch, st, nullptr);
+        else sho_forward(s, din, dout, nbatch, st, nullptr);
+        finish_out(s.st_out, adjoint ? bv : bm, st);
+    });
+}
+
+extern "C" int mmr_sho_destroy(mmr_sho* h) {
+    return guarded([&] { delete reinterpret_cast<ShoPlan*>(h); });
+}

@@ -1,0 +1,15 @@
+"""matmri_gb300 — GB300-native (sm_103a) MatMRI reconstruction hot path.
+
+Drop-in classes and functions with the reference's names and arguments:
+``nufftOp``, ``rcvrOp``, ``sampHighOrder``, ``mrSampFunc`` (+ ``mrSampOp``),
+``cgne``, ``powermethod``, ``bfista``, ``dwtND``.  All compute runs in
+``libmatmri_gb300.so`` (hand-written CUDA for sm_103a behind a C ABI); the
+package raises on import of an operator when the library is missing.
+"""
+from ._lib import MatmriError, load as load_library
+from .ops import nufftOp, rcvrOp, sampHighOrder
+from .sense import mrSampFunc, mrSampOp
+from .solvers import bfista, cgne, dwtND, powermethod
+
+__all__ = ["nufftOp", "rcvrOp", "sampHighOrder", "mrSampFunc", "mrSampOp", "cgne", "powermethod", "bfista",
+           "dwtND", "MatmriError", "load_library"]

@@ -1,0 +1,170 @@
+"""Seeded synthetic MRI inputs with the shapes of the benchmark workloads.
+
+No public dataset is named for these workloads and the reference's own
+image/coil/B0 blobs are not distributed, so every input is generated here
+from ``numpy.random.Generator(PCG64(seed))``:
+
+* random-ellipse phantoms (optionally with a smooth complex phase),
+* variable-density multi-interleave spirals ``k(tau) = 0.5 tau^1.5 e^{i(2 pi T tau + 2 pi j / n_int)}``,
+  ``T = N / (2 n_int R)`` turns, clipped to ``|k| < 0.5``,
+* ring-of-Gaussians coil maps with linear phase, root-sum-of-squares
+  normalised (the pattern of simulation/simRcvrSens.m:77-79),
+* analytic ``|k|`` density compensation (the spiral analogue of
+  trajectory/projection.m:15-16),
+* complex Gaussian noise at a given SNR,
+* high-order encoding inputs: spherical-harmonic phase time courses whose
+  non-linear terms are smooth cubics in time at +-5 % of the linear-term
+  phase at the FOV edge, a sum-of-Gaussians B0 map spanning +-100 Hz, and a
+  30 ms readout.
+
+Arrays follow MATLAB index semantics (image ``[N1, N2]``, samples ``[M]``,
+coil maps ``[N1, N2, C]``).
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+
+def rng(seed: int) -> np.random.Generator:
+    return np.random.Generator(np.random.PCG64(int(seed)))
+
+
+def ellipse_phantom(N: int, n_ellipses: int = 10, seed: int = 0, complex_phase: bool = False) -> np.ndarray:
+    g = rng(seed)
+    c = (np.arange(N) - N / 2) / (N / 2)                      # normalised coords in [-1, 1)
+    X, Y = np.meshgrid(c, c, indexing="ij")
+    img = np.zeros((N, N))
+    for _ in range(n_ellipses):
+        cx, cy = g.uniform(-0.6, 0.6, 2)
+        a, b = g.uniform(0.05, 0.45, 2)
+        th = g.uniform(0, math.pi)
+        val = g.uniform(0, 1)
+        xr = (X - cx) * math.cos(th) + (Y - cy) * math.sin(th)
+        yr = -(X - cx) * math.sin(th) + (Y - cy) * math.cos(th)
+        img += val * ((xr / a) ** 2 + (yr / b) ** 2 <= 1.0)
+    img = img.astype(np.complex128)
+    if complex_phase:
+        co = g.uniform(-1, 1, 6)
+        ph = co[0] + co[1] * X + co[2] * Y + co[3] * X * Y + co[4] * X ** 2 + co[5] * Y ** 2
+        ph = ph / max(np.abs(ph).max(), 1e-12) * (math.pi / 2)
+        img = img * np.exp(1j * ph)
+    return img
+
+
+def spiral(N: int, n_int: int, samples: int, R: float = 1.0) -> np.ndarray:
+    """kloc [n_int*samples, 2] in [-0.5, 0.5), interleave-major (MATLAB kloc(:, [kx ky]))."""
+    T = N / (2.0 * n_int * R)
+    tau = np.arange(samples) / samples
+    ks = []
+    for j in range(n_int):
+        k = 0.5 * tau ** 1.5 * np.exp(1j * (2 * math.pi * T * tau + 2 * math.pi * j / n_int))
+        r = np.abs(k)
+        k = np.where(r >= 0.5, k / np.maximum(r, 1e-30) * np.nextafter(0.5, 0), k)
+        ks.append(k)
+    k = np.concatenate(ks)
+    kl = np.stack([k.real, k.imag], axis=1)
+    return np.clip(kl, -0.5, np.nextafter(0.5, 0))
+
+
+def spiral_dcf(kloc: np.ndarray, N: int) -> np.ndarray:
+    r = np.sqrt((kloc ** 2).sum(axis=1))
+    d = np.maximum(r, 0.5 / N)
+    return d / d.max()
+
+
+def coil_maps(N: int, C: int, seed: int = 0, randomize: bool = False) -> np.ndarray:
+    g = rng(seed)
+    fov = 1.0
+    c = (np.arange(N) - N / 2) / N * fov
+    X, Y = np.meshgrid(c, c, indexing="ij")
+    radius = 0.6 * fov / 2
+    sigma = 0.35 * fov
+    maps = np.empty((N, N, C), dtype=np.complex128)
+    for ci in range(C):
+        rr = radius * (g.uniform(0.8, 1.2) if randomize else 1.0)
+        ss = sigma * (g.uniform(0.8, 1.2) if randomize else 1.0)
+        ang = 2 * math.pi * ci / C
+        cx, cy = rr * math.cos(ang), rr * math.sin(ang)
+        mag = np.exp(-((X - cx) ** 2 + (Y - cy) ** 2) / (2 * ss ** 2))
+        a, b = g.uniform(-math.pi, math.pi, 2) / fov
+        c0 = g.uniform(-math.pi, math.pi)
+        maps[:, :, ci] = mag * np.exp(1j * (a * X + b * Y + c0))
+    rss = np.sqrt((np.abs(maps) ** 2).sum(axis=2, keepdims=True))
+    return maps / rss
+
+
+def add_noise(y: np.ndarray, snr: float, seed: int) -> np.ndarray:
+    g = rng(seed)
+    sig = math.sqrt(np.mean(np.abs(y) ** 2)) / snr
+    return y + sig / math.sqrt(2) * (g.standard_normal(y.shape) + 1j * g.standard_normal(y.shape))
+
+
+def highorder_inputs(N: int = 128, M: int = 16384, fov: float = 0.22, readout: float = 30e-3,
+                     seed: int = 3000, n_int: int = 1):
+    """Inputs for ``sampHighOrder``: b0 [N,N] rad/s, t [M] s, phs_spha [16,M], phs_conc [4,M], grid."""
+    g = rng(seed)
+    c = (np.arange(N) - N / 2) * fov / N
+    X, Y = np.meshgrid(c, c, indexing="ij")
+    grid = {"x": X, "y": Y, "z": np.zeros_like(X)}
+    kl = spiral(N, n_int, M // n_int, 1.0)
+    t = np.linspace(0.0, readout, M)
+    spha = np.zeros((16, M))
+    spha[1] = kl[:, 0] * 2 * math.pi * N / fov
+    spha[2] = kl[:, 1] * 2 * math.pi * N / fov
+    lin_edge = np.abs(spha[1:3]).max() * (fov / 2)           # linear-term phase at the FOV edge (rad)
+    tn = t / readout
+    edge = fov / 2
+    # basisFuncHarm orders: n=1 (0th), 2-4 (1st), 5-9 (2nd), 10-16 (3rd)
+    order = [0, 1, 1, 1, 2, 2, 2, 2, 2, 3, 3, 3, 3, 3, 3, 3]
+    for n in range(16):
+        if n in (1, 2):
+            continue
+        co = g.uniform(-1, 1, 4)
+        poly = co[0] + co[1] * tn + co[2] * tn ** 2 + co[3] * tn ** 3
+        poly = poly / max(np.abs(poly).max(), 1e-12)
+        spha[n] = poly * 0.05 * lin_edge / (edge ** order[n])
+    conc = np.zeros((4, M))
+    b0 = np.zeros((N, N))
+    for _ in range(int(g.integers(3, 6))):
+        cx, cy = g.uniform(-0.6, 0.6, 2) * fov / 2
+        s = g.uniform(0.1, 0.3) * fov
+        b0 += g.uniform(-1, 1) * np.exp(-((X - cx) ** 2 + (Y - cy) ** 2) / (2 * s ** 2))
+    b0 = b0 - b0.min()
+    b0 = b0 / max(b0.max(), 1e-12) * 200.0 - 100.0         # +-100 Hz
+    b0 = 2 * math.pi * b0                                    # rad/s
+    return b0, t, spha, conc, grid
+
+
+# --- named workloads ---------------------------------------------------------------
+
+def regridding_case(seed: int = 1000):
+    """128^2 single-coil regridding: 16 x 2048 spiral, kwidth 4, os 2, |k| DCF, SNR 50."""
+    N = 128
+    img = ellipse_phantom(N, 10, seed)
+    kloc = spiral(N, 16, 2048, 1.0)
+    dcf = spiral_dcf(kloc, N)
+    return dict(N=N, img=img, kloc=kloc, dcf=dcf, os=2.0, kwidth=4, snr=50.0, seed=seed)
+
+
+def sense_case(N: int = 256, C: int = 32, n_int: int = 4, samples: int = 4096, R: float = 4.0,
+               seed: int = 2000, snr: float | None = None, randomize_coils: bool = False):
+    """256^2 x 32-coil CG-SENSE: 4 x 4096 spiral at R = 4, kwidth 4, os 2, complex phantom."""
+    img = ellipse_phantom(N, 10, seed, complex_phase=True)
+    kloc = spiral(N, n_int, samples, R)
+    maps = coil_maps(N, C, seed + 1, randomize=randomize_coils)
+    return dict(N=N, C=C, img=img, kloc=kloc, maps=maps, os=2.0, kwidth=4, snr=snr, seed=seed)
+
+
+def batched_cases(n_slices: int = 64, seed: int = 4000):
+    """64 uneven slices: N in {96,128,192,256}, C in {8,16,32}, 2-8 interleaves x 2048-4096 samples."""
+    g = rng(seed)
+    out = []
+    for s in range(n_slices):
+        N = int(g.choice([96, 128, 192, 256]))
+        C = int(g.choice([8, 16, 32]))
+        n_int = int(g.integers(2, 9))
+        samples = int(g.integers(2048, 4097))
+        out.append(sense_case(N, C, n_int, samples, R=max(1.0, 16.0 / n_int), seed=seed + 10 * s + 1))
+    return out

@@ -1,0 +1,319 @@
+#!/usr/bin/env python
+"""Benchmark: plain 2D CG-SENSE solves per second on one GB300.
+
+Workload (the reference metric's configuration): cgne, 30 iterations, image
+256 x 256 complex64 random-ellipse phantom, 32 ring-of-Gaussian coil maps
+with linear phase, variable-density spiral 4 interleaves x 4096 samples at
+R = 4, Kaiser-Bessel width 4, oversampling 2 (512 x 512 grid), FP32
+operators with FP64 CG scalars.  cgne runs with xChangeThresh = [] and
+resThresh = [] so that exactly 30 iterations run (1 adjoint + 32 normal
+operators per solve).  Inputs are seeded synthetic data of these shapes.
+
+A step is one full solve.  `value` times solves with the k-space data already
+in HBM (device pointers through the C ABI); `e2e` times the same solve
+through the C ABI with pinned HOST buffers (the data [16384 x 32] complex64
+copied in and the image [256 x 256] copied out inside the timed region).
+Between timed steps the L2 is flushed by writing a 512 MiB buffer (outside
+the per-step events).  `--impl reference` times the reference algorithm's CPU
+restatement on the host cores.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "uwobrainhack2026-matmri_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+N_IMG, N_COIL, N_INT, N_SAMP, ACCEL = 256, 32, 4, 4096, 4.0
+NIT = 30
+METRIC = "CG-SENSE solves/s (cgne 30 it, 256^2, 32 coils, 4x4096 spiral R=4)"
+WORKLOAD = "cg-sense 256x256, 32 coils, 4x4096 spiral R=4, kwidth 4, os 2, 30 cgne iterations"
+NORMALS_PER_SOLVE = NIT + 2          # initial residual + explicit residual at nit=0 + 30 iterations
+ADJOINTS_PER_SOLVE = 1
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def make_case(seed=2000):
+    from matmri_gb300 import synth
+    c = synth.sense_case(N_IMG, N_COIL, N_INT, N_SAMP, ACCEL, seed=seed)
+    return c
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons during the timed region."""
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [s.strip() for s in line.split(",")]
+            if len(parts) >= 7:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def cpu_baseline(case, reps=2):
+    """FP64 CPU restatement of the reference algorithm (oracle/) on all host cores.
+
+    Sample: `reps` applications of the 32-coil normal operator A'A plus one
+    adjoint, extrapolated to a 30-iteration solve (1 adjoint + 32 normal ops).
+    """
+    import oracle.nufft_ref as nr
+    from oracle.sense_ref import RcvrRef, mrsampfunc
+    cores = len(os.sched_getaffinity(0))
+    nr.FFT_WORKERS = cores
+    S = nr.NufftRef([N_IMG, N_IMG], case["kloc"], None, 2.0, 4)
+    R = RcvrRef(case["maps"])
+    x = case["img"]
+    t0 = time.perf_counter()
+    y = mrsampfunc(x, "notransp", S, R)
+    t_fwd = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        mrsampfunc(mrsampfunc(x, "notransp", S, R), "transp", S, R)
+    t_norm = (time.perf_counter() - t0) / reps
+    t_adj = max(t_norm - t_fwd, 1e-9)
+    t_solve = NORMALS_PER_SOLVE * t_norm + ADJOINTS_PER_SOLVE * t_adj
+    return {"value": 1.0 / t_solve, "unit": "solves/s", "cores": cores, "kind": "port",
+            "sample": f"{reps} applications of the 32-coil normal operator (FP64 scipy.sparse gridding + "
+                      f"scipy.fft with {cores} workers), extrapolated to 1 adjoint + {NORMALS_PER_SOLVE} normal "
+                      f"operators per solve; {t_norm:.3f} s per normal operator"}
+
+
+def run_reference(args):
+    ws, rank, _ = dist_env()
+    if rank != 0:
+        return
+    case = make_case()
+    for _ in range(args.warmup):
+        b = cpu_baseline(case, reps=1)
+    vals = []
+    for _ in range(args.steps):
+        b = cpu_baseline(case, reps=1)
+        vals.append(1.0 / b["value"])
+    t = sum(vals) / len(vals)
+    v = 1.0 / t
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "cores": b["cores"]},
+            "cpu_baseline": {"value": v, "unit": "solves/s", "cores": b["cores"], "kind": "port",
+                             "sample": b["sample"]},
+            "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def stage_bytes(cc, N, G, M, W):
+    """Algorithmic bytes per launch of each normal-operator stage (complex64 = 8 B)."""
+    img, grid, half = N * N * 8, G * G * 8, G * N * 8
+    return [
+        img + cc * img + cc * half,          # 0: image x maps x deapod -> first-axis FFT (writes G x N per coil)
+        cc * half + cc * grid,               # 1: second-axis FFT (G x N -> G x G per coil)
+        2 * cc * grid,                       # 2: fused interp -> weight -> spread (grid in, grid out)
+        cc * grid + cc * half,               # 3: first-axis FFT + crop (G x G -> N x G per coil)
+        cc * half + cc * img + 2 * img,      # 4: second-axis FFT + crop + deapod + conj maps + coil sum
+    ]
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import ctypes as C
+    import torch
+    import matmri_gb300 as mm
+    from matmri_gb300 import _lib
+    ws, rank, local = dist_env()
+    torch.cuda.set_device(local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    lib = _lib.load()
+
+    case = make_case(seed=2000 + rank)
+    S = mm.nufftOp([N_IMG, N_IMG], case["kloc"], None, 1, 2.0, 4)
+    R = mm.rcvrOp(case["maps"], 0)
+    A = mm.mrSampOp(S, R)
+    data = A(case["img"], "notransp")                 # synthetic k-space [M, C] (set-up, not timed)
+    M = data.shape[0]
+    dev = torch.device("cuda", local)
+    dt = torch.from_numpy(np.asfortranarray(data).T.copy()).to(dev).T   # column-major [M, C] on device
+    xt = torch.empty((N_IMG, N_IMG), dtype=torch.complex64, device=dev).T
+    dh = torch.from_numpy(np.ascontiguousarray(np.asfortranarray(data).T)).pin_memory()
+    xh = torch.empty((N_IMG, N_IMG), dtype=torch.complex64).pin_memory()
+    opts = _lib.CgneOpts()
+    _lib.check(lib.mmr_cgne_default_opts(C.byref(opts)))
+    opts.nit_max = NIT
+    opts.res_thresh = float("nan")
+    opts.x_change_thresh = float("nan")
+    stream = torch.cuda.current_stream(dev)
+    sp = stream.cuda_stream
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def solve(dev_ptrs=True):
+        if dev_ptrs:
+            r = lib.mmr_cgne_solve(A.handle, dt.data_ptr(), None, None, C.byref(opts), xt.data_ptr(), None, sp)
+        else:
+            r = lib.mmr_cgne_solve(A.handle, dh.data_ptr(), None, None, C.byref(opts), xh.data_ptr(), None, sp)
+        _lib.check(r)
+
+    def timed(n, dev_ptrs):
+        tot = 0.0
+        for _ in range(n):
+            flush.zero_()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            solve(dev_ptrs)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            tot += e0.elapsed_time(e1) / 1e3
+        return tot
+
+    # warm-up (graph capture, scratch sizing, clocks)
+    for _ in range(max(args.warmup, 3)):
+        solve(True)
+        solve(False)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    def max_over_ranks(v):
+        if ws > 1:
+            import torch.distributed as dist
+            t = torch.tensor([v], dtype=torch.float64, device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            return float(t.item())
+        return v
+
+    c0 = C.c_uint64()
+    _lib.check(lib.mmr_kernel_launches(C.byref(c0)))
+    with ClockSampler(local) as clk:
+        barrier()
+        t_dev = timed(args.steps, True)
+        barrier()
+    c1 = C.c_uint64()
+    _lib.check(lib.mmr_kernel_launches(C.byref(c1)))
+    barrier()
+    t_e2e = timed(args.steps, False)
+    barrier()
+    t_dev = max_over_ranks(t_dev)
+    t_e2e = max_over_ranks(t_e2e)
+    launches = int(c1.value - c0.value)
+
+    # live per-stage timing of the normal operator (CUDA events on the launching stream)
+    p = torch.from_numpy(np.asfortranarray(case["img"].astype(np.complex64)).T.copy()).to(dev).T
+    q = torch.empty_like(p)
+    ms = (C.c_double * 5)()
+    cnt = (C.c_int32 * 5)()
+    reps = 20
+    _lib.check(lib.mmr_sense_profile_normal(A.handle, p.data_ptr(), q.data_ptr(), reps, ms, cnt, sp))
+    cc, tile = A.get_tuning()
+    G = S.osN[0]
+    sb = stage_bytes(cc, N_IMG, G, M, 4)
+    total_ms = sum(ms[i] for i in range(5))
+    dom = max(range(5), key=lambda i: ms[i])
+    per_launch_s = ms[dom] / 1e3 / max(cnt[dom], 1)
+    achieved = sb[dom] / per_launch_s / 1e9
+    peak, peak_kind = peaks()
+    stage_names = ["fft_img_to_grid_axis0", "fft_axis1", "gridnorm_interp_spread", "fft_grid_axis0",
+                   "fft_axis1_coilsum"]
+
+    if rank == 0:
+        value = ws * args.steps / t_dev
+        line = {
+            "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_dev / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "c64 (FP64 CG scalars)", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "image": [N_IMG, N_IMG], "coils": N_COIL, "samples": M,
+                       "iterations": NIT, "coil_chunk": cc, "tile": tile, "grid": [G, G],
+                       "l2": "flushed between timed steps (512 MiB write, outside the per-step events)",
+                       "parallelism": f"replicas x{ws}"},
+            "e2e": {"value": ws * args.steps / t_e2e, "unit": "solves/s",
+                    "h2d_bytes_per_step": int(M * N_COIL * 8), "d2h_bytes_per_step": int(N_IMG * N_IMG * 8)},
+            "gpu_launches": launches,
+            "roofline": {"bound": "hbm", "kernel": stage_names[dom], "achieved": achieved, "peak": peak,
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                         "algorithmic_bytes_per_launch": sb[dom], "avg_launch_us": per_launch_s * 1e6,
+                         "stage_share": {stage_names[i]: round(ms[i] / total_ms, 4) for i in range(5)}},
+            "clocks": clk.summary(),
+        }
+        if not args.no_cpu_baseline:
+            line["cpu_baseline"] = cpu_baseline(case)
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -57,6 +57,9 @@ MMR_API int  mmr_abi_version(void);
 MMR_API int  mmr_last_error(char* buf, size_t len);
 /* Device properties used by the autotuner (SM count, smem per block). */
 MMR_API int  mmr_device_info(int* sm_count, int* smem_optin_bytes, int* cc_major, int* cc_minor);
+/* Kernels this library has launched in the process (eager launches plus the
+ * kernel nodes of every replayed CUDA graph). */
+MMR_API int  mmr_kernel_launches(uint64_t* count);
 
 /* ---- @nufftOp ------------------------------------------------------------
  * Replaces nufftOp(imN, kloc, dcf, useGPU, os, kwidth)
@@ -150,6 +153,14 @@ MMR_API int mmr_sense_create(const mmr_sense_desc* desc, mmr_sense** out);
 MMR_API int mmr_sense_apply(mmr_sense* a, int transp, const void* in, void* out, void* stream);
 /* A'*(A*x) with the fused gridding (used by cgne.m:215-218).             */
 MMR_API int mmr_sense_normal(mmr_sense* a, const void* in, void* out, void* stream);
+/* Runs the normal operator `reps` times with a CUDA event before every kernel
+ * and returns, per stage, the summed time (ms) and the number of launches:
+ * stage 0 first image->grid FFT pass (deapod + coil maps), 1 remaining
+ * image->grid passes, 2 gridding (fused interp/spread, or sampHighOrder
+ * encode), 3 grid->image passes before the last, 4 last pass (crop, deapod,
+ * conj maps, coil sum).  stage_ms / launches hold 5 entries.              */
+MMR_API int mmr_sense_profile_normal(mmr_sense* a, const void* in, void* out, int32_t reps,
+                                     double* stage_ms, int32_t* launches, void* stream);
 /* Tuning knobs chosen by the autotuner: coil chunk (0 = auto) and tile side. */
 MMR_API int mmr_sense_set_tuning(mmr_sense* a, int32_t coil_chunk, int32_t tile);
 MMR_API int mmr_sense_get_tuning(const mmr_sense* a, int32_t* coil_chunk, int32_t* tile);

@@ -86,7 +86,7 @@ def mrsampfunc(x, transp, samplingOp, R=None, opt=None):
         x_tik = x[nda:]
         x = x[:nda]
     if W is not None:
-        x = x * W
+        x = mtimes_bcast(W, x)
     if daNFull is not None:
         x = np.reshape(x, daNFull, order="F")
     if is_op:
@@ -106,6 +106,16 @@ def mrsampfunc(x, transp, samplingOp, R=None, opt=None):
     if hardReal:
         x = np.real(x)
     return x
+
+
+def mtimes_bcast(w, a):
+    """MATLAB implicit expansion of ``w .* a`` where ``w`` is a column vector
+    (e.g. per-sample weights [M x 1] against data [M x C])."""
+    w = np.asarray(w)
+    a = np.asarray(a)
+    if w.ndim == 1 and a.ndim > 1 and w.shape[0] == a.shape[0]:
+        w = w.reshape((-1,) + (1,) * (a.ndim - 1))
+    return w * a
 
 
 def _asub(Ain):
@@ -169,10 +179,10 @@ def cgne_ref(Ain, bin, x0=None, NitMax=None, opt=None, gam=None, Rin=None, W=Non
     def normal(v):
         av = A(v, "notransp")
         if W is not None:
-            av = W * av
+            av = mtimes_bcast(W, av)
         return A(av, "transp")
 
-    b = A(W * bin if W is not None else bin, "transp")                   # 136-140
+    b = A(mtimes_bcast(W, bin) if W is not None else bin, "transp")                   # 136-140
     if x0 is None:
         x0 = b                                                           # 143-145
     stopThresh = None

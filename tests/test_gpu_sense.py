@@ -73,7 +73,7 @@ def test_coil_chunks(mm, chunk):
 
 def test_opt_W_and_vectorised(mm):
     S, R, Sr, Rr, rng = _setup(mm, C=4, seed=7)
-    W = rng.uniform(0, 2, 3000)
+    W = rng.uniform(0, 2, 3000 * 4)      # vectorised data: W matches x(:) (mrSampFunc.m:126-128)
     opt = {"W": W, "imNFull": [64, 64], "daNFull": [3000, 4]}
     op = mm.mrSampOp(S, R, opt)
     y = crandn(rng, 3000 * 4)
@@ -162,7 +162,8 @@ def test_cgne_stopping_rules(mm, rule):
     assert len(rs) == len(rsr), (rule, len(rs), len(rsr))
     assert rel(x, xr) < 1e-4
     if rule == "noise":
-        assert abs(st - str_) / str_ < 1e-4
+        # cgne.m:305 zeroes stopThresh once the rule fires; both return that value
+        assert (st == str_ == 0) or abs(st - str_) / abs(str_) < 1e-4
 
 
 def test_cgne_partial_handle_and_torch(mm):

@@ -45,6 +45,7 @@ struct CgWorkspace {
     Staged sb, sxo;
     // graph cache
     cudaGraphExec_t g_norm = nullptr, g_expl = nullptr;
+    int k_norm = 0, k_expl = 0;   // kernel nodes per graph
     const void* key[8] = {nullptr};
     long long keyv[4] = {0};
     ~CgWorkspace() {
@@ -296,7 +297,8 @@ static unsigned red_grid(long long n) {
 static bool isset(double v) { return !std::isnan(v); }
 
 // Captures one iteration (explicit or not) on `st`.
-static cudaGraphExec_t capture_iter(SenseOp& a, CgWorkspace& w, bool expl, bool has_tik, bool has_gt) {
+static cudaGraphExec_t capture_iter(SenseOp& a, CgWorkspace& w, bool expl, bool has_tik, bool has_gt,
+                                    int& kernels) {
     cudaStream_t st = a.stream;
     CgState* sp = w.state.as<CgState>();
     double* hist = w.hist.as<double>();
@@ -310,6 +312,7 @@ static cudaGraphExec_t capture_iter(SenseOp& a, CgWorkspace& w, bool expl, bool 
     const float* tik = has_tik ? w.tik.as<float>() : nullptr;
     const float2* gt = has_gt ? w.gt.as<float2>() : nullptr;
     MMR_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+    set_capturing(true);
     try {
         sense_normal(a, p, Ap, st, active);
         cg_pap_kernel<<<g, 256, 0, st>>>(p, Ap, tik, n, sp);
@@ -322,13 +325,25 @@ static cudaGraphExec_t capture_iter(SenseOp& a, CgWorkspace& w, bool expl, bool 
         }
         cg_p_kernel<<<g, 256, 0, st>>>(p, res, n, sp);
     } catch (...) {
-        cudaGraph_t gr;
+        set_capturing(false);
+        cudaGraph_t gr = nullptr;
         cudaStreamEndCapture(st, &gr);
         if (gr) cudaGraphDestroy(gr);
         throw;
     }
+    set_capturing(false);
     cudaGraph_t gr = nullptr;
     MMR_CUDA(cudaStreamEndCapture(st, &gr));
+    size_t nn = 0;
+    MMR_CUDA(cudaGraphGetNodes(gr, nullptr, &nn));
+    std::vector<cudaGraphNode_t> nodes(nn);
+    MMR_CUDA(cudaGraphGetNodes(gr, nodes.data(), &nn));
+    kernels = 0;
+    for (auto nd : nodes) {
+        cudaGraphNodeType t;
+        MMR_CUDA(cudaGraphNodeGetType(nd, &t));
+        if (t == cudaGraphNodeTypeKernel) ++kernels;
+    }
     cudaGraphExec_t ex = nullptr;
     cudaError_t e = cudaGraphInstantiate(&ex, gr, 0);
     cudaGraphDestroy(gr);
@@ -442,8 +457,8 @@ static void cg_solve(SenseOp& a, const void* b_user, const void* x0_user, const 
         if (w.g_expl) cudaGraphExecDestroy(w.g_expl);
         w.g_norm = w.g_expl = nullptr;
         // one eager normal op sizes every scratch buffer before capture
-        w.g_norm = capture_iter(a, w, false, has_tik, has_gt);
-        w.g_expl = capture_iter(a, w, true, has_tik, has_gt);
+        w.g_norm = capture_iter(a, w, false, has_tik, has_gt, w.k_norm);
+        w.g_expl = capture_iter(a, w, true, has_tik, has_gt, w.k_expl);
         for (int i = 0; i < 8; ++i) w.key[i] = key[i];
         for (int i = 0; i < 4; ++i) w.keyv[i] = keyv[i];
     }
@@ -455,7 +470,11 @@ static void cg_solve(SenseOp& a, const void* b_user, const void* x0_user, const 
     int it = 0;
     while (it < limit) {
         const int end = std::min(limit, it + poll);
-        for (; it < end; ++it) MMR_CUDA(cudaGraphLaunch((it % expResN == 0) ? w.g_expl : w.g_norm, st));
+        for (; it < end; ++it) {
+            const bool ex = it % expResN == 0;
+            MMR_CUDA(cudaGraphLaunch(ex ? w.g_expl : w.g_norm, st));
+            add_launches(ex ? w.k_expl : w.k_norm);
+        }
         int fin = 0;
         MMR_CUDA(cudaMemcpyAsync(&fin, &sp->finished, sizeof(int), cudaMemcpyDeviceToHost, st));
         MMR_CUDA(cudaStreamSynchronize(st));
@@ -471,7 +490,8 @@ static void cg_solve(SenseOp& a, const void* b_user, const void* x0_user, const 
         hist->nit = fs.nit;
         hist->n = fs.nit + 1;
         hist->status = fs.status;
-        hist->stop_thresh = stop_thresh_out;
+        // cgne.m:305 sets stopThresh = 0 once the discrepancy rule has fired
+        hist->stop_thresh = h.has_stop ? fs.stop_thresh : stop_thresh_out;
         const int m = std::min(hist->capacity, fs.nit + 1);
         std::vector<double> hh((size_t)4 * cap);
         MMR_CUDA(cudaMemcpy(hh.data(), w.hist.p, hh.size() * sizeof(double), cudaMemcpyDeviceToHost));

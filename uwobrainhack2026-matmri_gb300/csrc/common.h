@@ -62,9 +62,22 @@ int guarded(F&& body) {
     }
 }
 
+// ------------------------------------------------- launch counting / profiling ----
+// Kernels launched by the library: eager launches are counted as they are
+// issued; launches recorded into a graph are counted when the graph replays.
+void note_launch();
+void set_capturing(bool on);
+void add_launches(uint64_t n);
+// Stage profiler: when active, prof_mark() records a CUDA event on `st`
+// tagged with the stage that starts there (stage < 0 closes the last one).
+void prof_mark(int stage, cudaStream_t st);
+void prof_begin();
+void prof_end(double* ms, int* count, int nstage);
+
 inline void check_launch(const char* what) {
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) MMR_THROW(MMR_ERR_CUDA, "launch of %s failed: %s", what, cudaGetErrorString(e));
+    note_launch();
 }
 
 // ----------------------------------------------------------- device buffer ----

@@ -207,6 +207,7 @@ static void launch_mode(const PassArgs& a, cudaStream_t st) {
         cfg.numAttrs = 0;
     }
     MMR_CUDA(cudaLaunchKernelEx(&cfg, kern, a));
+    note_launch();
 }
 
 void launch_fft_pass(int mode, const PassArgs& a, cudaStream_t st) {

@@ -875,6 +875,7 @@ void nufft_img_to_grid(NufftPlan& p, const float2* x, const float2* maps, float2
             a.maps = maps;
             a.lpc = (long long)p.N[1] * p.N[2];
         }
+        prof_mark(ax == 0 ? 0 : 1, st);
         launch_fft_pass(mode, a, st);
         ext[ax] = p.G[ax];
         src = dst;
@@ -922,6 +923,7 @@ void nufft_grid_to_img(NufftPlan& p, const float2* grid, const float2* maps, flo
         } else {
             a.outer = outer;
         }
+        prof_mark(last ? 4 : 3, st);
         launch_fft_pass(mode, a, st);
         ext[ax] = p.N[ax];
         src = dst;

@@ -183,14 +183,17 @@ void sense_normal(SenseOp& a, const float2* x, float2* y, cudaStream_t st, const
             rcvr_forward(*a.rcvr, x, a.s_img.as<float2>(), st, active);
             xin = a.s_img.as<float2>();
         }
+        prof_mark(2, st);
         sho_forward(*a.sho, xin, smp, nb, st, active);
         if (a.d_wnorm.p) {
             weight_kernel<<<(unsigned)cdiv(a.M * nb, 256), 256, 0, st>>>(smp, a.d_wnorm.as<float>(), smp, a.M, nb,
                                                                        a.w_bstride, active);
             check_launch("weight");
         }
+        prof_mark(2, st);
         if (a.rcvr) {
             sho_adjoint(*a.sho, smp, a.s_img.as<float2>(), a.C, st, active);
+            prof_mark(4, st);
             rcvr_adjoint(*a.rcvr, a.s_img.as<float2>(), y, st, active);
         } else {
             sho_adjoint(*a.sho, smp, y, 1, st, active);
@@ -207,6 +210,7 @@ void sense_normal(SenseOp& a, const float2* x, float2* y, cudaStream_t st, const
             const long long n = std::min<long long>(cc, a.C - c0);
             const float* w = wptr(a.d_wnorm, a.w_bstride * c0);
             nufft_img_to_grid(p, x, maps ? maps + c0 * a.Nimg : nullptr, a.s_grid.as<float2>(), n, st, active);
+            prof_mark(2, st);
             if (fused) {
                 nufft_grid_normal(p, a.s_grid.as<float2>(), a.s_grid2.as<float2>(), n, w, a.w_bstride, st, active);
             } else {
@@ -217,6 +221,7 @@ void sense_normal(SenseOp& a, const float2* x, float2* y, cudaStream_t st, const
                               active);
         }
     }
+    prof_mark(-1, st);
     if (a.tikreg != 0) {
         axpy_real_kernel<<<(unsigned)cdiv(a.Nimg, 256), 256, 0, st>>>(y, x, (float)(a.tikreg * a.tikreg), a.Nimg,
                                                                     active);
@@ -426,5 +431,37 @@ extern "C" int mmr_sense_destroy(mmr_sense* h) {
         cg_release(h->a);
         if (h->a.stream) cudaStreamDestroy(h->a.stream);
         delete h;
+    });
+}
+
+extern "C" int mmr_sense_profile_normal(mmr_sense* h, const void* in, void* out, int32_t reps, double* stage_ms,
+                                        int32_t* launches, void* stream) {
+    return guarded([&] {
+        MMR_REQUIRE(h && in && out && stage_ms && launches && reps >= 1, "bad argument");
+        SenseOp& a = h->a;
+        cudaStream_t st = as_stream(stream);
+        sense_set_weights(a, nullptr, false);
+        const size_t bimg = (size_t)a.Nimg * 8;
+        const float2* din = (const float2*)stage_in(a.st_in, in, bimg, st);
+        float2* dout = (float2*)stage_out(a.st_out, out, bimg);
+        sense_normal(a, din, dout, st, nullptr);   // sizes scratch outside the measurement
+        MMR_CUDA(cudaStreamSynchronize(st));
+        prof_begin();
+        try {
+            for (int r = 0; r < reps; ++r) sense_normal(a, din, dout, st, nullptr);
+        } catch (...) {
+            double d[5];
+            int c[5];
+            prof_end(d, c, 5);
+            throw;
+        }
+        double ms[5];
+        int cnt[5];
+        prof_end(ms, cnt, 5);
+        for (int i = 0; i < 5; ++i) {
+            stage_ms[i] = ms[i];
+            launches[i] = cnt[i];
+        }
+        finish_out(a.st_out, bimg, st);
     });
 }

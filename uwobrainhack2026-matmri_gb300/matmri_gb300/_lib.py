@@ -75,6 +75,9 @@ SIGNATURES = {
     "mmr_abi_version": (C.c_int, []),
     "mmr_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
     "mmr_device_info": (C.c_int, [C.POINTER(C.c_int)] * 4),
+    "mmr_kernel_launches": (C.c_int, [C.POINTER(C.c_uint64)]),
+    "mmr_sense_profile_normal": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_double),
+                                           C.POINTER(C.c_int32), C.c_void_p]),
     "mmr_nufft_create": (C.c_int, [C.POINTER(NufftDesc), C.POINTER(C.c_void_p)]),
     "mmr_nufft_set_dcf": (C.c_int, [C.c_void_p, C.POINTER(C.c_double)]),
     "mmr_nufft_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64), C.POINTER(C.c_double), C.POINTER(C.c_int64)]),

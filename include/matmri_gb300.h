@@ -161,9 +161,19 @@ MMR_API int mmr_sense_normal(mmr_sense* a, const void* in, void* out, void* stre
  * conj maps, coil sum).  stage_ms / launches hold 5 entries.              */
 MMR_API int mmr_sense_profile_normal(mmr_sense* a, const void* in, void* out, int32_t reps,
                                      double* stage_ms, int32_t* launches, void* stream);
-/* Tuning knobs chosen by the autotuner: coil chunk (0 = auto) and tile side. */
-MMR_API int mmr_sense_set_tuning(mmr_sense* a, int32_t coil_chunk, int32_t tile);
-MMR_API int mmr_sense_get_tuning(const mmr_sense* a, int32_t* coil_chunk, int32_t* tile);
+/* Tuning knobs chosen by the autotuner (0 = keep / automatic):
+ *   coil_chunk  coils per pipeline pass (1..16; their grids stay L2-resident)
+ *   tile        gridding tile side (8, 16, 32, 64)
+ *   coil_group  coils per CTA in the gridding kernels (1, 2, 4, 8)
+ *   item        max samples per gridding work item (>= 8)                 */
+typedef struct mmr_tuning {
+    int32_t coil_chunk;
+    int32_t tile;
+    int32_t coil_group;
+    int32_t item;
+} mmr_tuning;
+MMR_API int mmr_sense_set_tuning(mmr_sense* a, const mmr_tuning* t);
+MMR_API int mmr_sense_get_tuning(const mmr_sense* a, mmr_tuning* t);
 MMR_API int mmr_sense_destroy(mmr_sense* a);
 
 /* ---- cgne -------------------------------------------------------------------

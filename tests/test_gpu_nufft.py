@@ -114,11 +114,11 @@ def test_binned_path_tiles_agree(mm):
     x = crandn(rng, imN + [4])
     y = crandn(rng, (M, 4))
     R = mm.rcvrOp(np.ones(imN + [1], dtype=np.complex64), 0)
-    for tile in (8, 16, 32, 64):
+    for tile, cgrp, item in ((8, 1, 8), (16, 2, 16), (32, 4, 64), (64, 8, 256), (32, 8, 100000)):
         N = mm.nufftOp(imN, kloc, None, 1, 2.0, 4)
         op = mm.mrSampOp(N, None)
-        op.set_tuning(0, tile)
-        assert op.get_tuning()[1] == tile
+        op.set_tuning(0, tile, cgrp, item)
+        assert op.get_tuning()[1:] == (tile, cgrp, item)
         assert rel(N * x, ref.mtimes(x)) < TOL
         assert rel(N.H * y, ref.H.mtimes(y)) < TOL
 

@@ -14,9 +14,11 @@
 //    evaluates the W x W taps of a sample with one lane per tap and a
 //    warp-shuffle reduction;
 //  * spread2d_binned  — adjoint spreading; samples are pre-sorted into the
-//    tiles their footprint touches, each CTA owns one output tile,
-//    accumulates it in shared memory and flushes it with coalesced stores
-//    (no global atomics, no memset of the grid);
+//    tiles their footprint touches and split into work items of bounded size;
+//    each CTA accumulates its item in a shared-memory tile.  A tile served by
+//    one item is owned and flushed with coalesced plain stores (no memset);
+//    the few dense tiles (the centre of a variable-density trajectory) are
+//    zeroed first and their items add non-zero cells with vector reductions;
 //  * gridnorm2d_binned — the two fused for the normal operator
 //    C^H diag(w) C: interp from a staged tile + 2W halo, weight, spread into
 //    the owned tile; the samples never round-trip through HBM;
@@ -182,9 +184,32 @@ void nufft_set_dcf(NufftPlan& p, const double* dcf) {
     p.has_dcf = true;
 }
 
-void nufft_build_bins(NufftPlan& p, int Treq) {
+// Splits every tile's entry range [ptr[t], ptr[t+1]) into items of <= chunk entries.
+static void make_items(const std::vector<int>& ptr, int chunk, std::vector<int4>& items, std::vector<int>* heavy) {
+    items.clear();
+    if (heavy) heavy->clear();
+    const int ntile = (int)ptr.size() - 1;
+    for (int t = 0; t < ntile; ++t) {
+        const int n = ptr[t + 1] - ptr[t];
+        const int nit = (n + chunk - 1) / chunk;
+        const int hv = nit > 1 ? 1 : 0;
+        if (hv && heavy) heavy->push_back(t);
+        if (n == 0 && heavy) {   // empty tiles still own (and zero) their output region
+            items.push_back(make_int4(t, ptr[t], ptr[t], 0));
+            continue;
+        }
+        for (int k = 0; k < nit; ++k) {
+            const int e0 = ptr[t] + k * chunk, e1 = std::min(ptr[t + 1], e0 + chunk);
+            items.push_back(make_int4(t, e0, e1, hv));
+        }
+    }
+}
+
+void nufft_build_bins(NufftPlan& p, int Treq, int chunk) {
     p.use_bins = false;
     if (p.nd != 2) return;
+    MMR_REQUIRE(chunk >= 8, "work-item chunk must be >= 8");
+    p.bins.chunk = chunk;
     int T = Treq;
     while (T >= 8 && (p.G[0] < 2 * (T + 2 * p.W) || p.G[1] < 2 * (T + 2 * p.W))) T /= 2;
     if (T < 8 || T < p.W) return;
@@ -258,6 +283,16 @@ void nufft_build_bins(NufftPlan& p, int Treq) {
     b.pad_s.upload(ps);
     b.pad_lb.upload(plb);
     b.n_pad = (long long)ps.size();
+    std::vector<int4> items;
+    std::vector<int> heavy;
+    make_items(cnt, chunk, items, nullptr);
+    b.own_items.upload(items);
+    b.n_own_items = (int)items.size();
+    make_items(pptr, chunk, items, &heavy);
+    b.pad_items.upload(items);
+    b.n_pad_items = (int)items.size();
+    b.heavy.upload(heavy);
+    b.n_heavy = (int)heavy.size();
     p.use_bins = true;
     p.tmap_ptr = nullptr;   // invalidate descriptor caches (box depends on T)
 }
@@ -389,7 +424,7 @@ __device__ __forceinline__ float2 group_sum(float2 v) {
 
 // ------------------------------------------------------- binned 2D kernels ----
 struct Bin2DArgs {
-    const int* ptr;
+    const int4* items;       // {tile, e0, e1, heavy}
     const int* ent_s;
     const short2* ent_lb;
     const float* wts;        // [M][2][W]
@@ -411,9 +446,10 @@ __global__ void __launch_bounds__(256) interp2d_binned(const float2* __restrict_
     const int R = a.T + W;
     uint64_t* bar;
     float2* reg = tma_layout(sm4, &bar);
-    const int tile = blockIdx.x;
+    const int4 item = a.items[blockIdx.x];
+    const int tile = item.x;
     const int c0 = blockIdx.y * a.cg;
-    const int e0 = a.ptr[tile], e1 = a.ptr[tile + 1];
+    const int e0 = item.y, e1 = item.z;
     if (e0 == e1) return;
     const int tx = tile % a.ntx, ty = tile / a.ntx;
     mbar_init(bar);
@@ -456,6 +492,39 @@ __global__ void __launch_bounds__(256) interp2d_binned(const float2* __restrict_
     }
 }
 
+// Writes a CTA's accumulated tile: plain stores when the tile is owned by this
+// CTA, vector reductions of the non-zero cells into a pre-zeroed region when
+// several items share the tile.
+__device__ __forceinline__ void flush_tile(const float2* acc, float2* __restrict__ out, bool heavy, int T, int u0,
+                                           int v0, int te1, int te2, int c0, const Bin2DArgs& a) {
+    for (int i = threadIdx.x; i < a.cg * T * T; i += blockDim.x) {
+        const int c = i / (T * T), r = i - c * T * T, l2 = r / T, l1 = r - l2 * T;
+        if (l1 < te1 && l2 < te2 && c0 + c < a.nb) {
+            float2* d = out + (u0 + l1) + (long long)a.G1 * ((v0 + l2) + (long long)a.G2 * (c0 + c));
+            const float2 v = acc[i];
+            if (!heavy) *d = v;
+            else if (v.x != 0.f || v.y != 0.f) atomicAdd(d, v);
+        }
+    }
+}
+
+// Zeroes the output regions of the heavy tiles (all nb planes).
+__global__ void zero_tiles_kernel(float2* __restrict__ out, const int* __restrict__ tiles, int ntiles, int T, int ntx,
+                                  int G1, int G2, long long nb, const int* active) {
+    if (active && *active) return;
+    const long long per = (long long)T * T * nb;
+    const long long tot = per * ntiles;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < tot;
+         i += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(i / per);
+        const long long r = i - k * per;
+        const long long c = r / (T * T);
+        const int rr = (int)(r - c * T * T), l2 = rr / T, l1 = rr - l2 * T;
+        const int t = tiles[k], u0 = (t % ntx) * T, v0 = (t / ntx) * T;
+        if (u0 + l1 < G1 && v0 + l2 < G2) out[(u0 + l1) + (long long)G1 * ((v0 + l2) + (long long)G2 * c)] = make_float2(0.f, 0.f);
+    }
+}
+
 template <int W>
 __global__ void __launch_bounds__(256) spread2d_binned(const float2* __restrict__ y, float2* __restrict__ grid,
                                                        const Bin2DArgs a) {
@@ -464,14 +533,15 @@ __global__ void __launch_bounds__(256) spread2d_binned(const float2* __restrict_
     if (a.active && *a.active) return;
     float2* acc = reinterpret_cast<float2*>(sm4);
     const int T = a.T;
-    const int tile = blockIdx.x;
+    const int4 item = a.items[blockIdx.x];
+    const int tile = item.x;
     const int c0 = blockIdx.y * a.cg;
     const int tx = tile % a.ntx, ty = tile / a.ntx;
     const int u0 = tx * T, v0 = ty * T;
     const int te1 = min(T, a.G1 - u0), te2 = min(T, a.G2 - v0);
     for (int i = threadIdx.x; i < a.cg * T * T; i += blockDim.x) acc[i] = make_float2(0.f, 0.f);
     __syncthreads();
-    const int e0 = a.ptr[tile], e1 = a.ptr[tile + 1];
+    const int e0 = item.y, e1 = item.z;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
     const int grp = lane / TM::LPP, gl = lane % TM::LPP;
     const int npairs = (e1 - e0) * a.cg;
@@ -506,11 +576,7 @@ __global__ void __launch_bounds__(256) spread2d_binned(const float2* __restrict_
         }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < a.cg * T * T; i += blockDim.x) {
-        const int c = i / (T * T), r = i - c * T * T, l2 = r / T, l1 = r - l2 * T;
-        if (l1 < te1 && l2 < te2 && c0 + c < a.nb)
-            grid[(u0 + l1) + (long long)a.G1 * ((v0 + l2) + (long long)a.G2 * (c0 + c))] = acc[i];
-    }
+    flush_tile(acc, grid, item.w != 0, T, u0, v0, te1, te2, c0, a);
 }
 
 template <int W>
@@ -523,13 +589,14 @@ __global__ void __launch_bounds__(256) gridnorm2d_binned(const float2* __restric
     uint64_t* bar;
     float2* reg = tma_layout(sm4, &bar);
     float2* acc = reg + (size_t)a.cg * R * R;
-    const int tile = blockIdx.x;
+    const int4 item = a.items[blockIdx.x];
+    const int tile = item.x;
     const int c0 = blockIdx.y * a.cg;
     const int tx = tile % a.ntx, ty = tile / a.ntx;
     const int u0 = tx * T, v0 = ty * T;
     const int te1 = min(T, a.G1 - u0), te2 = min(T, a.G2 - v0);
     for (int i = threadIdx.x; i < a.cg * T * T; i += blockDim.x) acc[i] = make_float2(0.f, 0.f);
-    const int e0 = a.ptr[tile], e1 = a.ptr[tile + 1];
+    const int e0 = item.y, e1 = item.z;
     mbar_init(bar);
     if (e1 > e0) {
         if (!stage_region(reg, gin, &tmap, a.use_tma, bar, u0 - W, v0 - W, c0, a.cg, R, a.G1, a.G2, a.nb)) return;
@@ -588,11 +655,7 @@ __global__ void __launch_bounds__(256) gridnorm2d_binned(const float2* __restric
         }
     }
     __syncthreads();
-    for (int i = threadIdx.x; i < a.cg * T * T; i += blockDim.x) {
-        const int c = i / (T * T), r = i - c * T * T, l2 = r / T, l1 = r - l2 * T;
-        if (l1 < te1 && l2 < te2 && c0 + c < a.nb)
-            gout[(u0 + l1) + (long long)a.G1 * ((v0 + l2) + (long long)a.G2 * (c0 + c))] = acc[i];
-    }
+    flush_tile(acc, gout, item.w != 0, T, u0, v0, te1, te2, c0, a);
 }
 
 // ------------------------------------------------------------ generic kernels --
@@ -688,7 +751,7 @@ __global__ void spread_generic(const float2* __restrict__ y, float2* __restrict_
 // ---------------------------------------------------------------- dispatch ----
 static int pick_cg(const NufftPlan& p, long long nb, size_t per_coil_bytes, size_t fixed) {
     const size_t lim = (size_t)std::min(device_smem_optin(), 200 * 1024);
-    int cg = 8;
+    int cg = std::max(1, std::min(8, p.cg_pref));
     while (cg > 1 && fixed + per_coil_bytes * cg > lim) cg /= 2;
     while (cg > 1 && cg / 2 >= nb) cg /= 2;
     return cg;
@@ -698,7 +761,7 @@ static Bin2DArgs bin_args(const NufftPlan& p, bool own, const float* wfac, long 
                           bool tma, const int* active) {
     Bin2DArgs a;
     const BinLists& b = p.bins;
-    a.ptr = own ? b.own_ptr.as<int>() : b.pad_ptr.as<int>();
+    a.items = own ? b.own_items.as<int4>() : b.pad_items.as<int4>();
     a.ent_s = own ? b.own_s.as<int>() : b.pad_s.as<int>();
     a.ent_lb = own ? b.own_lb.as<short2>() : b.pad_lb.as<short2>();
     a.wts = p.d_w.as<float>();
@@ -765,12 +828,22 @@ void nufft_interp(NufftPlan& p, const float2* grid, float2* y, long long nb, con
     }
     const size_t smem = kTmaSmemExtra + (size_t)cg * R * R * 8;
     Bin2DArgs a = bin_args(p, true, wfac, wfb, nb, cg, true, active);
-    dim3 gridDim((unsigned)(p.bins.ntx * p.bins.nty), (unsigned)cdiv(nb, cg));
+    dim3 gridDim((unsigned)p.bins.n_own_items, (unsigned)cdiv(nb, cg));
+    if (p.bins.n_own_items == 0) return;
     MMR_W_DISPATCH(p.W, {
         set_smem(interp2d_binned<KW>, smem);
         interp2d_binned<KW><<<gridDim, 256, smem, st>>>(grid, y, a, p.tmap);
     });
     check_launch("interp2d_binned");
+}
+
+static void zero_heavy(NufftPlan& p, float2* out, long long nb, cudaStream_t st, const int* active) {
+    const BinLists& b = p.bins;
+    if (b.n_heavy == 0) return;
+    const long long tot = (long long)b.n_heavy * b.T * b.T * nb;
+    const unsigned g = (unsigned)std::min<long long>(cdiv(tot, 256), 4LL * device_sm_count());
+    zero_tiles_kernel<<<g, 256, 0, st>>>(out, b.heavy.as<int>(), b.n_heavy, b.T, b.ntx, p.G[0], p.G[1], nb, active);
+    check_launch("zero_tiles");
 }
 
 void nufft_spread(NufftPlan& p, const float2* y, float2* grid, long long nb, const float* wfac, long long wfb,
@@ -786,7 +859,8 @@ void nufft_spread(NufftPlan& p, const float2* y, float2* grid, long long nb, con
     const int cg = pick_cg(p, nb, (size_t)T * T * 8, 0);
     const size_t smem = (size_t)cg * T * T * 8;
     Bin2DArgs a = bin_args(p, false, wfac, wfb, nb, cg, false, active);
-    dim3 gridDim((unsigned)(p.bins.ntx * p.bins.nty), (unsigned)cdiv(nb, cg));
+    dim3 gridDim((unsigned)p.bins.n_pad_items, (unsigned)cdiv(nb, cg));
+    zero_heavy(p, grid, nb, st, active);
     MMR_W_DISPATCH(p.W, {
         set_smem(spread2d_binned<KW>, smem);
         spread2d_binned<KW><<<gridDim, 256, smem, st>>>(y, grid, a);
@@ -817,7 +891,8 @@ void nufft_grid_normal(NufftPlan& p, const float2* gin, float2* gout, long long 
     }
     const size_t smem = kTmaSmemExtra + (size_t)cg * (R * R + T * T) * 8;
     Bin2DArgs a = bin_args(p, false, wfac, wfb, nb, cg, true, active);
-    dim3 gridDim((unsigned)(p.bins.ntx * p.bins.nty), (unsigned)cdiv(nb, cg));
+    dim3 gridDim((unsigned)p.bins.n_pad_items, (unsigned)cdiv(nb, cg));
+    zero_heavy(p, gout, nb, st, active);
     MMR_W_DISPATCH(p.W, {
         set_smem(gridnorm2d_binned<KW>, smem);
         gridnorm2d_binned<KW><<<gridDim, 256, smem, st>>>(gin, gout, a, g_norm_map);

@@ -8,11 +8,21 @@
 namespace mmr {
 
 // Binned sample lists for one tile size (2D fast path).
+//
+// Work is split into items of at most `chunk` entries so that the dense centre
+// of a variable-density trajectory is spread over many CTAs.  A tile whose
+// padded list needs several items is "heavy": its output region is zeroed
+// first and every item adds its non-zero cells with vector reductions; a
+// light tile (one item) owns its region and writes it with plain stores.
 struct BinLists {
     int T = 0;                 // tile side (grid cells)
+    int chunk = 0;             // max entries per work item
     int ntx = 0, nty = 0;
     DevBuf own_ptr, own_s, own_lb;   // interp: each sample once (tile containing its base cell)
     DevBuf pad_ptr, pad_s, pad_lb;   // spread/normal: every tile its footprint touches
+    DevBuf own_items, pad_items;     // int4 {tile, e0, e1, heavy}
+    DevBuf heavy;                    // int: heavy tile ids
+    int n_own_items = 0, n_pad_items = 0, n_heavy = 0;
     long long n_own = 0, n_pad = 0;
     int max_own = 0, max_pad = 0;
 };
@@ -38,6 +48,7 @@ struct NufftPlan {
     const float2* tw[3] = {nullptr, nullptr, nullptr};
     BinLists bins;                // valid when use_bins
     bool use_bins = false;
+    int cg_pref = 4;              // coils per CTA in the gridding kernels (autotuned)
     // scratch
     DevBuf s_tmp, s_grid, s_grid2;
     Staged st_in, st_out;
@@ -55,7 +66,7 @@ struct NufftPlan {
 
 void nufft_plan_build(NufftPlan& p, const mmr_nufft_desc& d);
 void nufft_set_dcf(NufftPlan& p, const double* dcf);
-void nufft_build_bins(NufftPlan& p, int T);
+void nufft_build_bins(NufftPlan& p, int T, int chunk = 64);
 
 // Operations on device buffers (all on `st`).  `active` (nullable) makes every
 // kernel a no-op while *active != 0 (device-resident solver termination).

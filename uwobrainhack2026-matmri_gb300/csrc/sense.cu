@@ -402,26 +402,38 @@ extern "C" int mmr_sense_normal(mmr_sense* h, const void* in, void* out, void* s
     });
 }
 
-extern "C" int mmr_sense_set_tuning(mmr_sense* h, int32_t coil_chunk, int32_t tile) {
+extern "C" int mmr_sense_set_tuning(mmr_sense* h, const mmr_tuning* t) {
     return guarded([&] {
-        MMR_REQUIRE(h, "NULL op");
+        MMR_REQUIRE(h && t, "NULL argument");
         SenseOp& a = h->a;
-        MMR_REQUIRE(coil_chunk >= 0 && coil_chunk <= 16, "coil_chunk must be 0..16");
-        a.coil_chunk = coil_chunk;
-        if (tile > 0 && a.nufft && a.nufft->nd == 2 && tile != a.nufft->bins.T) {
-            MMR_REQUIRE(tile == 8 || tile == 16 || tile == 32 || tile == 64, "tile must be 8, 16, 32 or 64");
-            nufft_build_bins(*a.nufft, tile);
+        MMR_REQUIRE(t->coil_chunk >= 0 && t->coil_chunk <= 16, "coil_chunk must be 0..16");
+        MMR_REQUIRE(t->coil_group == 0 || t->coil_group == 1 || t->coil_group == 2 || t->coil_group == 4 ||
+                        t->coil_group == 8, "coil_group must be 1, 2, 4 or 8");
+        MMR_REQUIRE(t->item == 0 || t->item >= 8, "item must be >= 8");
+        if (t->coil_chunk > 0) a.coil_chunk = t->coil_chunk;
+        if (a.nufft) {
+            NufftPlan& p = *a.nufft;
+            if (t->coil_group > 0) p.cg_pref = t->coil_group;
+            const int tile = t->tile > 0 ? t->tile : p.bins.T;
+            const int item = t->item > 0 ? t->item : p.bins.chunk;
+            if (p.nd == 2 && (tile != p.bins.T || item != p.bins.chunk)) {
+                MMR_REQUIRE(tile == 8 || tile == 16 || tile == 32 || tile == 64, "tile must be 8, 16, 32 or 64");
+                nufft_build_bins(p, tile, item);
+            }
+            a.tile = p.use_bins ? p.bins.T : 0;
         }
-        a.tile = a.nufft && a.nufft->use_bins ? a.nufft->bins.T : 0;
         cg_release(a);   // graphs captured with the old tuning are stale
     });
 }
 
-extern "C" int mmr_sense_get_tuning(const mmr_sense* h, int32_t* coil_chunk, int32_t* tile) {
+extern "C" int mmr_sense_get_tuning(const mmr_sense* h, mmr_tuning* t) {
     return guarded([&] {
-        MMR_REQUIRE(h, "NULL op");
-        if (coil_chunk) *coil_chunk = sense_chunk(h->a);
-        if (tile) *tile = h->a.nufft && h->a.nufft->use_bins ? h->a.nufft->bins.T : 0;
+        MMR_REQUIRE(h && t, "NULL argument");
+        const SenseOp& a = h->a;
+        t->coil_chunk = sense_chunk(a);
+        t->tile = a.nufft && a.nufft->use_bins ? a.nufft->bins.T : 0;
+        t->coil_group = a.nufft ? a.nufft->cg_pref : 0;
+        t->item = a.nufft && a.nufft->use_bins ? a.nufft->bins.chunk : 0;
     });
 }
 

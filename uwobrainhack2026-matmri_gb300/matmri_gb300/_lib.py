@@ -43,6 +43,10 @@ class SenseDesc(C.Structure):
                 ("W", C.POINTER(C.c_float)), ("w_per_coil", C.c_int32), ("tikreg", C.c_double)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("coil_chunk", C.c_int32), ("tile", C.c_int32), ("coil_group", C.c_int32), ("item", C.c_int32)]
+
+
 class CgneOpts(C.Structure):
     _fields_ = [("nit_max", C.c_int32), ("res_thresh", C.c_double), ("res_change_thresh", C.c_double),
                 ("x_change_thresh", C.c_double), ("exp_res_n", C.c_int32), ("nse_thresh_fact", C.c_double),
@@ -93,8 +97,8 @@ SIGNATURES = {
     "mmr_sense_create": (C.c_int, [C.POINTER(SenseDesc), C.POINTER(C.c_void_p)]),
     "mmr_sense_apply": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mmr_sense_normal": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),
-    "mmr_sense_set_tuning": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32]),
-    "mmr_sense_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32)]),
+    "mmr_sense_set_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
+    "mmr_sense_get_tuning": (C.c_int, [C.c_void_p, C.POINTER(Tuning)]),
     "mmr_sense_destroy": (C.c_int, [C.c_void_p]),
     "mmr_cgne_default_opts": (C.c_int, [C.POINTER(CgneOpts)]),
     "mmr_cgne_solve": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_float), C.POINTER(CgneOpts),

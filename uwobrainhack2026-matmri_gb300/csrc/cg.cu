@@ -102,9 +102,28 @@ __device__ __forceinline__ bool last_block(CgState* st) {
     return false;
 }
 
+// The state is read with independent L2 loads (st.global.cg / ld.global.cg,
+// written by other blocks' atomics) into a register copy, updated, and
+// written back; one thread of the last block runs this.
+static_assert(sizeof(CgState) % 8 == 0, "CgState must be a whole number of 8-byte words");
+__device__ __forceinline__ void state_load(CgState& s, const CgState* st) {
+    const unsigned long long* src = reinterpret_cast<const unsigned long long*>(st);
+    unsigned long long* dst = reinterpret_cast<unsigned long long*>(&s);
+#pragma unroll
+    for (int i = 0; i < (int)(sizeof(CgState) / 8); ++i) dst[i] = __ldcg(src + i);
+}
+__device__ __forceinline__ void state_store(CgState* st, const CgState& s) {
+    unsigned long long* dst = reinterpret_cast<unsigned long long*>(st);
+    const unsigned long long* src = reinterpret_cast<const unsigned long long*>(&s);
+#pragma unroll
+    for (int i = 0; i < (int)(sizeof(CgState) / 8); ++i) __stcg(dst + i, src[i]);
+}
+
 // Scalar epilogue of one iteration (cgne.m:252-335).
 __device__ void cg_finalize(CgState* st, double* hist, bool expl) {
-    volatile CgState* vs = st;
+    CgState ls;
+    state_load(ls, st);
+    CgState* vs = &ls;
     const int nit = vs->nit;
     const int cap = vs->cap;
     double* hr = hist;
@@ -154,8 +173,9 @@ __device__ void cg_finalize(CgState* st, double* hist, bool expl) {
     vs->pAp_re = vs->pAp_im = 0.0;
     vs->acc_res = vs->acc_xn = vs->acc_xd = vs->acc_mse = 0.0;
     vs->counter = 0;
-    __threadfence();
     if (finished) vs->finished = 1;
+    state_store(st, ls);
+    __threadfence();
 }
 
 // res = b - Ax - tik.*x0 ; p = res ; histories at index 0 (cgne.m:164-207)

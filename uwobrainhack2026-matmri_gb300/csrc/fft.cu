@@ -61,12 +61,13 @@ __global__ void __launch_bounds__(256) fft_pass_kernel(const PassArgs a) {
     extern __shared__ float4 sm4[];
     float2* sm = reinterpret_cast<float2*>(sm4);
     if (a.active && *a.active) return;
-    const int L = a.L, B = a.B, ls = L;
+    const int L = a.L, B = a.B;
+    int lgB = 0;
+    while ((1 << lgB) < B) ++lgB;
+    const int ls = padded_len(L);
     float2* buf0 = sm;
     float2* buf1 = sm + B * ls;
-    float2* twd = sm + 2 * B * ls;
     const int tid = threadIdx.x, nt = blockDim.x;
-    for (int i = tid; i < L; i += nt) twd[i] = a.tw[i];
 
     // ---- tile decomposition
     const bool contiguous = (MODE != PASS_ADJ_COMBINE) && a.inner == 1;
@@ -80,75 +81,59 @@ __global__ void __launch_bounds__(256) fft_pass_kernel(const PassArgs a) {
         q0 = ((long long)blockIdx.x % ntq) * B;
         if (MODE == PASS_ADJ_COMBINE) coil = blockIdx.y;
     }
-    auto line_valid = [&](int b) -> bool {
-        return contiguous ? (l0 + b < a.outer) : (q0 + b < a.inner);
+    auto line_valid = [&](int b) -> bool { return contiguous ? (l0 + b < a.outer) : (q0 + b < a.inner); };
+
+    // first stage input: natural index n <- input position t = (n - in_start) mod L (zero padding beyond nin)
+    auto ld = [&](int b, int n) -> float2 {
+        int t = n - a.in_start;
+        t += (t < 0) ? L : 0;
+        if (t >= a.nin || !line_valid(b)) return make_float2(0.f, 0.f);
+        float2 v;
+        if (MODE == PASS_FWD_IMG) {
+            const long long l = l0 + b;
+            const float2 x = a.in[t + (long long)a.nin * (l % a.lpc)];
+            v = a.maps ? cmul(x, a.maps[t + (long long)a.nin * l]) : x;
+        } else if (contiguous) {
+            v = a.in[t + (long long)a.nin * (l0 + b)];
+        } else {
+            const long long oo = (MODE == PASS_ADJ_COMBINE) ? coil : o;
+            v = a.in[(q0 + b) + a.inner * (t + (long long)a.nin * oo)];
+        }
+        if (a.in_fac) v = cmul(v, a.in_fac[t]);
+        return v;
     };
 
-    // ---- zero the positions that carry no input (zero padding)
-    const int nz = L - a.nin;
-    for (int idx = tid; idx < B * nz; idx += nt) {
-        const int b = idx / nz, t = a.nin + idx % nz;
-        int nat = a.in_start + t;
-        nat -= (nat >= L) ? L : 0;
-        buf0[b * ls + nat] = make_float2(0.f, 0.f);
-    }
-    // ---- load (coalesced along the contiguous index)
-    for (int idx = tid; idx < B * a.nin; idx += nt) {
-        int b, t;
-        if (contiguous) { b = idx / a.nin; t = idx - b * a.nin; }
-        else { t = idx / B; b = idx - t * B; }
-        float2 v = make_float2(0.f, 0.f);
-        if (line_valid(b)) {
-            if (MODE == PASS_FWD_IMG) {
-                const long long l = l0 + b;
-                const float2 x = a.in[t + (long long)a.nin * (l % a.lpc)];
-                v = a.maps ? cmul(x, a.maps[t + (long long)a.nin * l]) : x;
-            } else if (contiguous) {
-                v = a.in[t + (long long)a.nin * (l0 + b)];
-            } else {
-                const long long oo = (MODE == PASS_ADJ_COMBINE) ? coil : o;
-                v = a.in[(q0 + b) + a.inner * (t + (long long)a.nin * oo)];
-            }
-            if (a.in_fac) v = cmul(v, a.in_fac[t]);
-        }
-        int nat = a.in_start + t;
-        nat -= (nat >= L) ? L : 0;
-        buf0[b * ls + nat] = v;
-    }
-    __syncthreads();
-
-    float2* res = fft_lines<SIGN>(buf0, buf1, twd, a.f, B, ls);
-    float2* spare = (res == buf0) ? buf1 : buf0;
-
     if (MODE != PASS_ADJ_COMBINE) {
-        for (int idx = tid; idx < B * a.nout; idx += nt) {
-            int b, t;
-            if (contiguous) { b = idx / a.nout; t = idx - b * a.nout; }
-            else { t = idx / B; b = idx - t * B; }
-            if (!line_valid(b)) continue;
-            int nat = a.out_start + t;
-            nat -= (nat >= L) ? L : 0;
-            float2 v = cscale(res[b * ls + nat], a.scale);
+        // last stage output: natural index n -> output position t = (n - out_start) mod L (crop beyond nout)
+        auto stf = [&](int b, int n, float2 v) {
+            int t = n - a.out_start;
+            t += (t < 0) ? L : 0;
+            if (t >= a.nout || !line_valid(b)) return;
+            v = cscale(v, a.scale);
             if (a.out_fac) v = cmul(v, a.out_fac[t]);
             if (contiguous) a.out[t + (long long)a.nout * (l0 + b)] = v;
             else a.out[(q0 + b) + a.inner * (t + (long long)a.nout * o)] = v;
-        }
+        };
+        fft_lines<SIGN>(buf0, buf1, a.tw, a.f, B, lgB, ls, !contiguous, ld, stf);
         return;
     }
 
-    // ---- ADJ_COMBINE: conj-map multiply, then deterministic coil sum over the cluster
-    for (int idx = tid; idx < B * a.nout; idx += nt) {
-        const int t = idx / B, b = idx - t * B;
-        float2 v = make_float2(0.f, 0.f);
+    // ---- ADJ_COMBINE: crop, deapod, conj(maps) into a staging tile, then a deterministic
+    //      coil sum across the thread-block cluster through distributed shared memory
+    float2* stg = sm + 2 * B * ls;
+    auto stc = [&](int b, int n, float2 v) {
+        int t = n - a.out_start;
+        t += (t < 0) ? L : 0;
+        if (t >= a.nout) return;
+        float2 r = make_float2(0.f, 0.f);
         if (line_valid(b)) {
-            int nat = a.out_start + t;
-            nat -= (nat >= L) ? L : 0;
-            v = cscale(res[b * ls + nat], a.scale);
-            if (a.out_fac) v = cmul(v, a.out_fac[t]);
-            if (a.maps) v = cmulc(v, a.maps[(q0 + b) + a.inner * (t + (long long)a.nout * coil)]);
+            r = cscale(v, a.scale);
+            if (a.out_fac) r = cmul(r, a.out_fac[t]);
+            if (a.maps) r = cmulc(r, a.maps[(q0 + b) + a.inner * (t + (long long)a.nout * coil)]);
         }
-        spare[idx] = v;
-    }
+        stg[t * B + b] = r;
+    };
+    fft_lines<SIGN>(buf0, buf1, a.tw, a.f, B, lgB, ls, true, ld, stc);
     cg::cluster_group cl = cg::this_cluster();
     cl.sync();
     const int cs = (int)cl.num_blocks();
@@ -157,15 +142,15 @@ __global__ void __launch_bounds__(256) fft_pass_kernel(const PassArgs a) {
     const int per = (tot + cs - 1) / cs;
     const int e0 = rank * per, e1 = min(tot, e0 + per);
     for (int idx = e0 + tid; idx < e1; idx += nt) {
-        float2 s = make_float2(0.f, 0.f);
+        float2 sum = make_float2(0.f, 0.f);
         for (int r = 0; r < cs; ++r) {
-            const float2* rem = cl.map_shared_rank(spare, r);
-            s = cadd(s, rem[idx]);
+            const float2* rem = cl.map_shared_rank(stg, r);
+            sum = cadd(sum, rem[idx]);
         }
         const int t = idx / B, b = idx - t * B;
         if (q0 + b < a.inner) {
             float2* dst = a.out + (q0 + b) + a.inner * (long long)t;
-            *dst = a.accumulate ? cadd(*dst, s) : s;
+            *dst = a.accumulate ? cadd(*dst, sum) : sum;
         }
     }
     cl.sync();
@@ -173,7 +158,8 @@ __global__ void __launch_bounds__(256) fft_pass_kernel(const PassArgs a) {
 
 template <int MODE, int SIGN>
 static void launch_mode(const PassArgs& a, cudaStream_t st) {
-    const size_t smem = (size_t)(2 * a.B * a.L + a.L) * sizeof(float2);
+    const size_t smem = (size_t)(2 * a.B * padded_len(a.L) + (MODE == PASS_ADJ_COMBINE ? a.B * a.L : 0)) *
+                        sizeof(float2);
     auto kern = fft_pass_kernel<MODE, SIGN>;
     static bool attr_done = false;   // one per instantiation
     if (!attr_done) {
@@ -212,6 +198,7 @@ static void launch_mode(const PassArgs& a, cudaStream_t st) {
 
 void launch_fft_pass(int mode, const PassArgs& a, cudaStream_t st) {
     MMR_REQUIRE(a.nin <= a.L && a.nout <= a.L && a.nin > 0 && a.nout > 0, "bad FFT pass extents");
+    MMR_REQUIRE(a.B >= 1 && (a.B & (a.B - 1)) == 0, "lines per block must be a power of two");
     if (mode == PASS_ADJ_COMBINE) MMR_REQUIRE(a.outer >= 1 && a.outer <= 16, "cluster coil count must be 1..16");
     if (a.sign < 0) {
         if (mode == PASS_PLAIN) launch_mode<PASS_PLAIN, -1>(a, st);

@@ -52,7 +52,7 @@ struct PassArgs {
     int nout = 0, out_start = 0;
     int sign = -1;                  // -1: e^{-i} (fft), +1: e^{+i} (ifft)
     float scale = 1.f;
-    int B = 1;                      // lines per block
+    int B = 1;                      // lines per block (power of two)
     int accumulate = 0;             // ADJ_COMBINE: out += (1) or out = (0)
     FftFactors f;
 };
@@ -140,48 +140,82 @@ __device__ __forceinline__ void dftR(float2* v) {
     else dft_odd<R, SIGN>(v);
 }
 
-// One Stockham stage for all B lines held in `src` (line stride `ls`), into `dst`.
-template <int R, int SIGN>
+// Shared-memory index with one pad slot per 16 entries: breaks the stride-R
+// bank conflicts of the Stockham scatter.
+__device__ __forceinline__ int pidx(int i) { return i + (i >> 4); }
+__host__ __device__ __forceinline__ int padded_len(int L) { return L + (L >> 4) + 1; }
+
+// One Stockham stage over B lines.  FIRST reads its inputs through `ld(b, n)`
+// (natural index n, straight from global memory); LAST hands its outputs to
+// `stf(b, n, v)`; the stages in between read `src` and write `dst` (shared
+// memory, line stride ls, padded indices).  `bfast`: consecutive threads
+// take consecutive lines (strided axes), else consecutive butterflies.
+template <int R, int SIGN, bool FIRST, bool LAST, class Ld, class St>
 __device__ __forceinline__ void stockham_stage(const float2* __restrict__ src, float2* __restrict__ dst,
-                                               const float2* __restrict__ tw, int L, int Ns, int B, int ls) {
+                                               const float2* __restrict__ tw, int L, int Ns, int B, int lgB, int ls,
+                                               bool bfast, const Ld& ld, const St& stf) {
     const int nbf = L / R;
     const int tws = L / (Ns * R);
     for (int w = threadIdx.x; w < nbf * B; w += blockDim.x) {
-        const int b = w / nbf;
-        const int j = w - b * nbf;
+        int b, j;
+        if (bfast) { b = w & (B - 1); j = w >> lgB; }
+        else { b = w / nbf; j = w - b * nbf; }
         const int k = j % Ns;
-        const float2* s = src + b * ls;
         float2 v[R];
+        if (FIRST) {
 #pragma unroll
-        for (int r = 0; r < R; ++r) v[r] = s[j + r * nbf];
-        if (Ns > 1) {
+            for (int r = 0; r < R; ++r) v[r] = ld(b, j + r * nbf);
+        } else {
+            const float2* s = src + b * ls;
+#pragma unroll
+            for (int r = 0; r < R; ++r) v[r] = s[pidx(j + r * nbf)];
+        }
+        if (!FIRST && Ns > 1) {
 #pragma unroll
             for (int r = 1; r < R; ++r) {
-                float2 t = tw[r * k * tws];
+                float2 t = __ldg(tw + r * k * tws);
                 if (SIGN > 0) t.y = -t.y;
                 v[r] = cmul(v[r], t);
             }
         }
         dftR<R, SIGN>(v);
-        float2* d = dst + b * ls + (j / Ns) * Ns * R + k;
+        const int base = (j / Ns) * Ns * R + k;
+        if (LAST) {
 #pragma unroll
-        for (int r = 0; r < R; ++r) d[r * Ns] = v[r];
+            for (int r = 0; r < R; ++r) stf(b, base + r * Ns, v[r]);
+        } else {
+            float2* d = dst + b * ls;
+#pragma unroll
+            for (int r = 0; r < R; ++r) d[pidx(base + r * Ns)] = v[r];
+        }
     }
 }
 
-// Runs all stages; returns the buffer (a or b) holding the result.
-template <int SIGN>
-__device__ float2* fft_lines(float2* a, float2* b, const float2* tw, const FftFactors& f, int B, int ls) {
+template <int R, int SIGN, class Ld, class St>
+__device__ __forceinline__ void run_stage(int s, int nstage, const float2* src, float2* dst, const float2* tw, int L,
+                                          int Ns, int B, int lgB, int ls, bool bfast, const Ld& ld, const St& stf) {
+    const bool first = s == 0, last = s == nstage - 1;
+    if (first && last) stockham_stage<R, SIGN, true, true>(src, dst, tw, L, Ns, B, lgB, ls, bfast, ld, stf);
+    else if (first) stockham_stage<R, SIGN, true, false>(src, dst, tw, L, Ns, B, lgB, ls, bfast, ld, stf);
+    else if (last) stockham_stage<R, SIGN, false, true>(src, dst, tw, L, Ns, B, lgB, ls, bfast, ld, stf);
+    else stockham_stage<R, SIGN, false, false>(src, dst, tw, L, Ns, B, lgB, ls, bfast, ld, stf);
+}
+
+// Runs all stages of B length-L transforms: input from ld, output to stf,
+// intermediates ping-pong between a and b (each B * ls float2).
+template <int SIGN, class Ld, class St>
+__device__ void fft_lines(float2* a, float2* b, const float2* tw, const FftFactors& f, int B, int lgB, int ls,
+                          bool bfast, const Ld& ld, const St& stf) {
     int Ns = 1;
     for (int s = 0; s < f.nstage; ++s) {
         const int R = f.radix[s];
         switch (R) {
-            case 8: stockham_stage<8, SIGN>(a, b, tw, f.L, Ns, B, ls); break;
-            case 4: stockham_stage<4, SIGN>(a, b, tw, f.L, Ns, B, ls); break;
-            case 2: stockham_stage<2, SIGN>(a, b, tw, f.L, Ns, B, ls); break;
-            case 3: stockham_stage<3, SIGN>(a, b, tw, f.L, Ns, B, ls); break;
-            case 5: stockham_stage<5, SIGN>(a, b, tw, f.L, Ns, B, ls); break;
-            case 7: stockham_stage<7, SIGN>(a, b, tw, f.L, Ns, B, ls); break;
+            case 8: run_stage<8, SIGN>(s, f.nstage, a, b, tw, f.L, Ns, B, lgB, ls, bfast, ld, stf); break;
+            case 4: run_stage<4, SIGN>(s, f.nstage, a, b, tw, f.L, Ns, B, lgB, ls, bfast, ld, stf); break;
+            case 2: run_stage<2, SIGN>(s, f.nstage, a, b, tw, f.L, Ns, B, lgB, ls, bfast, ld, stf); break;
+            case 3: run_stage<3, SIGN>(s, f.nstage, a, b, tw, f.L, Ns, B, lgB, ls, bfast, ld, stf); break;
+            case 5: run_stage<5, SIGN>(s, f.nstage, a, b, tw, f.L, Ns, B, lgB, ls, bfast, ld, stf); break;
+            case 7: run_stage<7, SIGN>(s, f.nstage, a, b, tw, f.L, Ns, B, lgB, ls, bfast, ld, stf); break;
             default: break;
         }
         __syncthreads();
@@ -190,7 +224,6 @@ __device__ float2* fft_lines(float2* a, float2* b, const float2* tw, const FftFa
         b = t;
         Ns *= R;
     }
-    return a;
 }
 
 // Launch a pass (host). `cluster` > 1 only for PASS_ADJ_COMBINE.

@@ -458,36 +458,38 @@ __global__ void __launch_bounds__(256) interp2d_binned(const float2* __restrict_
         return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
     const int grp = lane / TM::LPP, gl = lane % TM::LPP;
-    const int npairs = (e1 - e0) * a.cg;
-    for (int pb = warp * TM::PPW; pb < npairs; pb += nwarp * TM::PPW) {
-        const int pi = pb + grp;
-        float2 acc = make_float2(0.f, 0.f);
-        int s = 0, c = 0;
-        const bool valid = pi < npairs;
-        if (valid) {
-            const int e = e0 + pi / a.cg;
-            c = pi % a.cg;
-            s = a.ent_s[e];
-            const short2 lb = a.ent_lb[e];
-            const float* w = a.wts + (size_t)s * 2 * W;
-            const float2* rc = reg + (size_t)c * R * R;
+    // warp per entry: the entry's taps are decoded once, then reused for every coil
+    for (int e = e0 + warp; e < e1; e += nwarp) {
+        const int s = a.ent_s[e];
+        const short2 lb = a.ent_lb[e];
+        const float* w = a.wts + (size_t)s * 2 * W;
+        float wt[TM::TPL];
+        int ro[TM::TPL];
+#pragma unroll
+        for (int i = 0; i < TM::TPL; ++i) {
+            const int k = gl + i * TM::LPP;
+            const int ta = k % W, tb = k / W;
+            const bool ok = k < TM::TAPS;
+            wt[i] = ok ? w[ta] * w[W + tb] : 0.f;
+            ro[i] = ok ? (lb.y + tb + 1) * R + (lb.x + ta + 1) : 0;
+        }
+        for (int cb = 0; cb < a.cg; cb += TM::PPW) {
+            const int c = cb + grp;
+            const bool cv = c < a.cg;
+            const float2* rc = reg + (size_t)(cv ? c : 0) * R * R;
+            float2 v = make_float2(0.f, 0.f);
 #pragma unroll
             for (int i = 0; i < TM::TPL; ++i) {
-                const int k = gl + i * TM::LPP;
-                if (k < TM::TAPS) {
-                    const int ta = k % W, tb = k / W;
-                    const float wt = w[ta] * w[W + tb];
-                    const float2 g = rc[(lb.y + tb + 1) * R + (lb.x + ta + 1)];
-                    acc.x += wt * g.x;
-                    acc.y += wt * g.y;
-                }
+                const float2 g = rc[ro[i]];
+                v.x += wt[i] * g.x;
+                v.y += wt[i] * g.y;
             }
-        }
-        acc = group_sum<TM::LPP>(acc);
-        if (valid && gl == 0 && c0 + c < a.nb) {
-            float f = 1.f;
-            if (a.wfac) f = a.wfac[s + a.wfac_bstride * (c0 + c)];
-            y[s + a.M * (c0 + c)] = make_float2(acc.x * f, acc.y * f);
+            v = group_sum<TM::LPP>(v);
+            if (cv && gl == 0 && c0 + c < a.nb) {
+                float f = 1.f;
+                if (a.wfac) f = a.wfac[s + a.wfac_bstride * (c0 + c)];
+                y[s + a.M * (c0 + c)] = make_float2(v.x * f, v.y * f);
+            }
         }
     }
 }
@@ -508,20 +510,17 @@ __device__ __forceinline__ void flush_tile(const float2* acc, float2* __restrict
     }
 }
 
-// Zeroes the output regions of the heavy tiles (all nb planes).
-__global__ void zero_tiles_kernel(float2* __restrict__ out, const int* __restrict__ tiles, int ntiles, int T, int ntx,
-                                  int G1, int G2, long long nb, const int* active) {
+// Zeroes the output regions of the heavy tiles: block (k, c) clears tile tiles[k] of plane c.
+__global__ void __launch_bounds__(256) zero_tiles_kernel(float2* __restrict__ out, const int* __restrict__ tiles,
+                                                         int T, int ntx, int G1, int G2, const int* active) {
     if (active && *active) return;
-    const long long per = (long long)T * T * nb;
-    const long long tot = per * ntiles;
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < tot;
-         i += (long long)gridDim.x * blockDim.x) {
-        const int k = (int)(i / per);
-        const long long r = i - k * per;
-        const long long c = r / (T * T);
-        const int rr = (int)(r - c * T * T), l2 = rr / T, l1 = rr - l2 * T;
-        const int t = tiles[k], u0 = (t % ntx) * T, v0 = (t / ntx) * T;
-        if (u0 + l1 < G1 && v0 + l2 < G2) out[(u0 + l1) + (long long)G1 * ((v0 + l2) + (long long)G2 * c)] = make_float2(0.f, 0.f);
+    const int t = tiles[blockIdx.x];
+    const int u0 = (t % ntx) * T, v0 = (t / ntx) * T;
+    const int te1 = min(T, G1 - u0), te2 = min(T, G2 - v0);
+    float2* o = out + (long long)G1 * G2 * blockIdx.y;
+    for (int i = threadIdx.x; i < T * T; i += blockDim.x) {
+        const int l2 = i / T, l1 = i - l2 * T;
+        if (l1 < te1 && l2 < te2) o[(u0 + l1) + (long long)G1 * (v0 + l2)] = make_float2(0.f, 0.f);
     }
 }
 
@@ -544,33 +543,37 @@ __global__ void __launch_bounds__(256) spread2d_binned(const float2* __restrict_
     const int e0 = item.y, e1 = item.z;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
     const int grp = lane / TM::LPP, gl = lane % TM::LPP;
-    const int npairs = (e1 - e0) * a.cg;
     constexpr int off0 = -W / 2 + 1;
-    for (int pb = warp * TM::PPW; pb < npairs; pb += nwarp * TM::PPW) {
-        const int pi = pb + grp;
-        if (pi >= npairs) continue;
-        const int e = e0 + pi / a.cg, c = pi % a.cg;
-        if (c0 + c >= a.nb) continue;
+    for (int e = e0 + warp; e < e1; e += nwarp) {
         const int s = a.ent_s[e];
         const short2 lb = a.ent_lb[e];
-        float2 v = y[s + a.M * (c0 + c)];
-        if (a.wfac) {
-            const float f = a.wfac[s + a.wfac_bstride * (c0 + c)];
-            v.x *= f;
-            v.y *= f;
-        }
         const float* w = a.wts + (size_t)s * 2 * W;
-        float2* ac = acc + (size_t)c * T * T;
+        float wt[TM::TPL];
+        int ao[TM::TPL];
 #pragma unroll
         for (int i = 0; i < TM::TPL; ++i) {
             const int k = gl + i * TM::LPP;
-            if (k < TM::TAPS) {
-                const int ta = k % W, tb = k / W;
-                const int l1 = lb.x + off0 + ta, l2 = lb.y + off0 + tb;
-                if (l1 >= 0 && l1 < te1 && l2 >= 0 && l2 < te2) {
-                    const float wt = w[ta] * w[W + tb];
-                    atomicAdd(&ac[l2 * T + l1].x, wt * v.x);
-                    atomicAdd(&ac[l2 * T + l1].y, wt * v.y);
+            const int ta = k % W, tb = k / W;
+            const int l1 = lb.x + off0 + ta, l2 = lb.y + off0 + tb;
+            const bool ok = k < TM::TAPS && l1 >= 0 && l1 < te1 && l2 >= 0 && l2 < te2;
+            wt[i] = ok ? w[ta] * w[W + tb] : 0.f;
+            ao[i] = ok ? l2 * T + l1 : -1;
+        }
+        for (int cb = 0; cb < a.cg; cb += TM::PPW) {
+            const int c = cb + grp;
+            if (c >= a.cg || c0 + c >= a.nb) continue;
+            float2 v = y[s + a.M * (c0 + c)];
+            if (a.wfac) {
+                const float f = a.wfac[s + a.wfac_bstride * (c0 + c)];
+                v.x *= f;
+                v.y *= f;
+            }
+            float2* ac = acc + (size_t)c * T * T;
+#pragma unroll
+            for (int i = 0; i < TM::TPL; ++i) {
+                if (ao[i] >= 0) {
+                    atomicAdd(&ac[ao[i]].x, wt[i] * v.x);
+                    atomicAdd(&ac[ao[i]].y, wt[i] * v.y);
                 }
             }
         }
@@ -604,52 +607,49 @@ __global__ void __launch_bounds__(256) gridnorm2d_binned(const float2* __restric
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
     const int grp = lane / TM::LPP, gl = lane % TM::LPP;
-    const int npairs = (e1 - e0) * a.cg;
     constexpr int off0 = -W / 2 + 1;
-    for (int pb = warp * TM::PPW; pb < npairs; pb += nwarp * TM::PPW) {
-        const int pi = pb + grp;
-        const bool valid = pi < npairs;
-        int e = e0, c = 0, s = 0;
-        short2 lb = make_short2(0, 0);
-        if (valid) {
-            e = e0 + pi / a.cg;
-            c = pi % a.cg;
-            s = a.ent_s[e];
-            lb = a.ent_lb[e];
-        }
+    // warp per entry: decode the taps once (region offsets, accumulator offsets,
+    // weights), then interp -> weight -> spread for every coil of the group
+    for (int e = e0 + warp; e < e1; e += nwarp) {
+        const int s = a.ent_s[e];
+        const short2 lb = a.ent_lb[e];
         const float* w = a.wts + (size_t)s * 2 * W;
-        const float2* rc = reg + (size_t)c * R * R;
-        float2 v = make_float2(0.f, 0.f);
         float wt[TM::TPL];
+        int ro[TM::TPL], ao[TM::TPL];
 #pragma unroll
         for (int i = 0; i < TM::TPL; ++i) {
             const int k = gl + i * TM::LPP;
-            wt[i] = 0.f;
-            if (valid && k < TM::TAPS) {
-                const int ta = k % W, tb = k / W;
-                wt[i] = w[ta] * w[W + tb];
-                const float2 g = rc[(lb.y + off0 + tb + W) * R + (lb.x + off0 + ta + W)];
+            const int ta = k % W, tb = k / W;
+            const bool ok = k < TM::TAPS;
+            const int l1 = lb.x + off0 + ta, l2 = lb.y + off0 + tb;
+            wt[i] = ok ? w[ta] * w[W + tb] : 0.f;
+            ro[i] = ok ? (l2 + W) * R + (l1 + W) : 0;
+            ao[i] = (ok && l1 >= 0 && l1 < te1 && l2 >= 0 && l2 < te2) ? l2 * T + l1 : -1;
+        }
+        for (int cb = 0; cb < a.cg; cb += TM::PPW) {
+            const int c = cb + grp;
+            const bool cv = c < a.cg && c0 + c < a.nb;
+            const float2* rc = reg + (size_t)(c < a.cg ? c : 0) * R * R;
+            float2 v = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int i = 0; i < TM::TPL; ++i) {
+                const float2 g = rc[ro[i]];
                 v.x += wt[i] * g.x;
                 v.y += wt[i] * g.y;
             }
-        }
-        v = group_sum<TM::LPP>(v);
-        if (!valid || c0 + c >= a.nb) continue;
-        if (a.wfac) {
-            const float f = a.wfac[s + a.wfac_bstride * (c0 + c)];
-            v.x *= f;
-            v.y *= f;
-        }
-        float2* ac = acc + (size_t)c * T * T;
+            v = group_sum<TM::LPP>(v);
+            if (!cv) continue;
+            if (a.wfac) {
+                const float f = a.wfac[s + a.wfac_bstride * (c0 + c)];
+                v.x *= f;
+                v.y *= f;
+            }
+            float2* ac = acc + (size_t)c * T * T;
 #pragma unroll
-        for (int i = 0; i < TM::TPL; ++i) {
-            const int k = gl + i * TM::LPP;
-            if (k < TM::TAPS) {
-                const int ta = k % W, tb = k / W;
-                const int l1 = lb.x + off0 + ta, l2 = lb.y + off0 + tb;
-                if (l1 >= 0 && l1 < te1 && l2 >= 0 && l2 < te2) {
-                    atomicAdd(&ac[l2 * T + l1].x, wt[i] * v.x);
-                    atomicAdd(&ac[l2 * T + l1].y, wt[i] * v.y);
+            for (int i = 0; i < TM::TPL; ++i) {
+                if (ao[i] >= 0) {
+                    atomicAdd(&ac[ao[i]].x, wt[i] * v.x);
+                    atomicAdd(&ac[ao[i]].y, wt[i] * v.y);
                 }
             }
         }
@@ -840,9 +840,8 @@ void nufft_interp(NufftPlan& p, const float2* grid, float2* y, long long nb, con
 static void zero_heavy(NufftPlan& p, float2* out, long long nb, cudaStream_t st, const int* active) {
     const BinLists& b = p.bins;
     if (b.n_heavy == 0) return;
-    const long long tot = (long long)b.n_heavy * b.T * b.T * nb;
-    const unsigned g = (unsigned)std::min<long long>(cdiv(tot, 256), 4LL * device_sm_count());
-    zero_tiles_kernel<<<g, 256, 0, st>>>(out, b.heavy.as<int>(), b.n_heavy, b.T, b.ntx, p.G[0], p.G[1], nb, active);
+    zero_tiles_kernel<<<dim3((unsigned)b.n_heavy, (unsigned)nb), 256, 0, st>>>(out, b.heavy.as<int>(), b.T, b.ntx,
+                                                                           p.G[0], p.G[1], active);
     check_launch("zero_tiles");
 }
 
@@ -901,6 +900,12 @@ void nufft_grid_normal(NufftPlan& p, const float2* gin, float2* gout, long long 
 }
 
 // ------------------------------------------------------------- FFT pipelines --
+static int pow2_floor(int v) {
+    int r = 1;
+    while (r * 2 <= v) r *= 2;
+    return r;
+}
+
 static PassArgs base_pass(const NufftPlan& p, int axis, int sign) {
     PassArgs a;
     a.L = p.G[axis];
@@ -908,7 +913,7 @@ static PassArgs base_pass(const NufftPlan& p, int axis, int sign) {
     a.tw = p.tw[axis];
     a.sign = sign;
     a.scale = (float)(1.0 / std::sqrt((double)p.G[axis]));
-    a.B = std::max(1, std::min(16, 2048 / a.L));
+    a.B = pow2_floor(std::max(1, std::min(p.fft_lines, 4096 / a.L)));
     return a;
 }
 
@@ -993,7 +998,7 @@ void nufft_grid_to_img(NufftPlan& p, const float2* grid, const float2* maps, flo
             a.maps = maps;
             a.outer = nb;          // coils summed by the cluster
             a.accumulate = accumulate ? 1 : 0;
-            a.B = std::max(1, std::min<int>(8, (int)std::min<long long>(inner, 2048 / a.L)));
+            a.B = pow2_floor(std::max(1, (int)std::min<long long>(std::min<long long>(p.fft_lines, inner), 4096 / a.L)));
             if (inner == 1) a.B = 1;
         } else {
             a.outer = outer;
@@ -1050,7 +1055,7 @@ static void toep_passes(NufftPlan& p, const float2* in, float2* out, long long n
         a.tw = p.ttw[ax];
         a.sign = sign;
         a.scale = (float)(1.0 / std::sqrt((double)L[ax]));
-        a.B = std::max(1, std::min(16, 2048 / a.L));
+        a.B = pow2_floor(std::max(1, std::min(16, 2048 / a.L)));
         long long inner = 1, outer = nb;
         int outn = (nin_mode == 1) ? p.N[ax] : L[ax];
         for (int k = 0; k < ax; ++k) inner *= (nin_mode == 1 ? p.N[k] : L[k]);

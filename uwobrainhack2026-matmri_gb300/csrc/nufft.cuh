@@ -49,6 +49,7 @@ struct NufftPlan {
     BinLists bins;                // valid when use_bins
     bool use_bins = false;
     int cg_pref = 4;              // coils per CTA in the gridding kernels (autotuned)
+    int fft_lines = 8;            // lines per CTA in the FFT passes (autotuned, power of two)
     // scratch
     DevBuf s_tmp, s_grid, s_grid2;
     Staged st_in, st_out;

@@ -56,12 +56,12 @@ const float2* fft_twiddles(int L) {
     return d;
 }
 
-template <int MODE, int SIGN>
+template <int MODE, int SIGN, int LC>
 __global__ void __launch_bounds__(256) fft_pass_kernel(const PassArgs a) {
     extern __shared__ float4 sm4[];
     float2* sm = reinterpret_cast<float2*>(sm4);
     if (a.active && *a.active) return;
-    const int L = a.L, B = a.B;
+    const int L = LC ? LC : a.L, B = a.B;
     int lgB = 0;
     while ((1 << lgB) < B) ++lgB;
     const int ls = padded_len(L);
@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(256) fft_pass_kernel(const PassArgs a) {
             if (contiguous) a.out[t + (long long)a.nout * (l0 + b)] = v;
             else a.out[(q0 + b) + a.inner * (t + (long long)a.nout * o)] = v;
         };
-        fft_lines<SIGN>(buf0, buf1, a.tw, a.f, B, lgB, ls, !contiguous, ld, stf);
+        run_fft<LC, SIGN>(buf0, buf1, a.tw, a.f, B, lgB, ls, !contiguous, ld, stf);
         return;
     }
 
@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(256) fft_pass_kernel(const PassArgs a) {
         }
         stg[t * B + b] = r;
     };
-    fft_lines<SIGN>(buf0, buf1, a.tw, a.f, B, lgB, ls, true, ld, stc);
+    run_fft<LC, SIGN>(buf0, buf1, a.tw, a.f, B, lgB, ls, true, ld, stc);
     cg::cluster_group cl = cg::this_cluster();
     cl.sync();
     const int cs = (int)cl.num_blocks();
@@ -156,11 +156,11 @@ __global__ void __launch_bounds__(256) fft_pass_kernel(const PassArgs a) {
     cl.sync();
 }
 
-template <int MODE, int SIGN>
+template <int MODE, int SIGN, int LC>
 static void launch_mode(const PassArgs& a, cudaStream_t st) {
     const size_t smem = (size_t)(2 * a.B * padded_len(a.L) + (MODE == PASS_ADJ_COMBINE ? a.B * a.L : 0)) *
                         sizeof(float2);
-    auto kern = fft_pass_kernel<MODE, SIGN>;
+    auto kern = fft_pass_kernel<MODE, SIGN, LC>;
     static bool attr_done = false;   // one per instantiation
     if (!attr_done) {
         MMR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
@@ -196,18 +196,31 @@ static void launch_mode(const PassArgs& a, cudaStream_t st) {
     note_launch();
 }
 
+template <int LC>
+static void launch_len(int mode, const PassArgs& a, cudaStream_t st) {
+    static_assert(LC == 0 || fft_has_cplan(LC), "no compile-time plan");
+    if (a.sign < 0) {
+        if (mode == PASS_PLAIN) launch_mode<PASS_PLAIN, -1, LC>(a, st);
+        else if (mode == PASS_FWD_IMG) launch_mode<PASS_FWD_IMG, -1, LC>(a, st);
+        else launch_mode<PASS_ADJ_COMBINE, -1, LC>(a, st);
+    } else {
+        if (mode == PASS_PLAIN) launch_mode<PASS_PLAIN, 1, LC>(a, st);
+        else if (mode == PASS_FWD_IMG) launch_mode<PASS_FWD_IMG, 1, LC>(a, st);
+        else launch_mode<PASS_ADJ_COMBINE, 1, LC>(a, st);
+    }
+}
+
 void launch_fft_pass(int mode, const PassArgs& a, cudaStream_t st) {
     MMR_REQUIRE(a.nin <= a.L && a.nout <= a.L && a.nin > 0 && a.nout > 0, "bad FFT pass extents");
     MMR_REQUIRE(a.B >= 1 && (a.B & (a.B - 1)) == 0, "lines per block must be a power of two");
     if (mode == PASS_ADJ_COMBINE) MMR_REQUIRE(a.outer >= 1 && a.outer <= 16, "cluster coil count must be 1..16");
-    if (a.sign < 0) {
-        if (mode == PASS_PLAIN) launch_mode<PASS_PLAIN, -1>(a, st);
-        else if (mode == PASS_FWD_IMG) launch_mode<PASS_FWD_IMG, -1>(a, st);
-        else launch_mode<PASS_ADJ_COMBINE, -1>(a, st);
-    } else {
-        if (mode == PASS_PLAIN) launch_mode<PASS_PLAIN, 1>(a, st);
-        else if (mode == PASS_FWD_IMG) launch_mode<PASS_FWD_IMG, 1>(a, st);
-        else launch_mode<PASS_ADJ_COMBINE, 1>(a, st);
+    switch (a.L) {
+        case 512: launch_len<512>(mode, a, st); break;
+        case 384: launch_len<384>(mode, a, st); break;
+        case 256: launch_len<256>(mode, a, st); break;
+        case 192: launch_len<192>(mode, a, st); break;
+        case 128: launch_len<128>(mode, a, st); break;
+        default: launch_len<0>(mode, a, st); break;
     }
 }
 

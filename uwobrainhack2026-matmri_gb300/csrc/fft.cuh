@@ -226,6 +226,82 @@ __device__ void fft_lines(float2* a, float2* b, const float2* tw, const FftFacto
     }
 }
 
+// ---- compile-time radix plans for the oversampled grid lengths of the workloads
+// (2 x {64, 96, 128, 192, 256}); other lengths use the runtime path above.
+__host__ __device__ constexpr int cnstage(int L) {
+    return (L == 512 || L == 256 || L == 192 || L == 128) ? 3 : (L == 384 ? 4 : 0);
+}
+__host__ __device__ constexpr int cradix(int L, int s) {
+    return L == 512 ? 8
+         : L == 256 ? (s < 2 ? 8 : 4)
+         : L == 384 ? (s < 2 ? 8 : (s == 2 ? 2 : 3))
+         : L == 192 ? (s < 2 ? 8 : 3)
+         : L == 128 ? (s < 1 ? 8 : 4)
+         : 1;
+}
+__host__ __device__ constexpr int cns(int L, int s) { return s == 0 ? 1 : cns(L, s - 1) * cradix(L, s - 1); }
+__host__ __device__ constexpr bool fft_has_cplan(int L) { return cnstage(L) > 0; }
+
+template <int L, int S, int SIGN, class Ld, class St>
+__device__ __forceinline__ void cstage(const float2* __restrict__ src, float2* __restrict__ dst,
+                                       const float2* __restrict__ tw, int B, int lgB, int ls, bool bfast, const Ld& ld,
+                                       const St& stf) {
+    constexpr int R = cradix(L, S);
+    constexpr int Ns = cns(L, S);
+    constexpr bool FIRST = S == 0, LAST = S == cnstage(L) - 1;
+    constexpr int nbf = L / R;
+    constexpr int tws = L / (Ns * R);
+    for (int w = threadIdx.x; w < nbf * B; w += blockDim.x) {
+        int b, j;
+        if (bfast) { b = w & (B - 1); j = w >> lgB; }
+        else { b = w / nbf; j = w - b * nbf; }
+        const int k = j % Ns;
+        float2 v[R];
+        if (FIRST) {
+#pragma unroll
+            for (int r = 0; r < R; ++r) v[r] = ld(b, j + r * nbf);
+        } else {
+            const float2* s = src + b * ls;
+#pragma unroll
+            for (int r = 0; r < R; ++r) v[r] = s[pidx(j + r * nbf)];
+#pragma unroll
+            for (int r = 1; r < R; ++r) {
+                float2 t = __ldg(tw + r * k * tws);
+                if (SIGN > 0) t.y = -t.y;
+                v[r] = cmul(v[r], t);
+            }
+        }
+        dftR<R, SIGN>(v);
+        const int base = (j / Ns) * Ns * R + k;
+        if (LAST) {
+#pragma unroll
+            for (int r = 0; r < R; ++r) stf(b, base + r * Ns, v[r]);
+        } else {
+            float2* d = dst + b * ls;
+#pragma unroll
+            for (int r = 0; r < R; ++r) d[pidx(base + r * Ns)] = v[r];
+        }
+    }
+}
+
+template <int L, int S, int SIGN, class Ld, class St>
+__device__ __forceinline__ void cstages(float2* a, float2* b, const float2* tw, int B, int lgB, int ls, bool bfast,
+                                        const Ld& ld, const St& stf) {
+    if constexpr (S < cnstage(L)) {
+        cstage<L, S, SIGN>(a, b, tw, B, lgB, ls, bfast, ld, stf);
+        __syncthreads();
+        cstages<L, S + 1, SIGN>(b, a, tw, B, lgB, ls, bfast, ld, stf);
+    }
+}
+
+// LC = compile-time length (0: runtime plan f).
+template <int LC, int SIGN, class Ld, class St>
+__device__ __forceinline__ void run_fft(float2* a, float2* b, const float2* tw, const FftFactors& f, int B, int lgB,
+                                        int ls, bool bfast, const Ld& ld, const St& stf) {
+    if constexpr (LC == 0) fft_lines<SIGN>(a, b, tw, f, B, lgB, ls, bfast, ld, stf);
+    else cstages<LC, 0, SIGN>(a, b, tw, B, lgB, ls, bfast, ld, stf);
+}
+
 // Launch a pass (host). `cluster` > 1 only for PASS_ADJ_COMBINE.
 void launch_fft_pass(int mode, const PassArgs& a, cudaStream_t st);
 

@@ -370,17 +370,22 @@ __device__ __forceinline__ bool stage_region(float2* reg, const float2* __restri
         const bool ok = mbar_wait(bar, 0);
         return ok;
     }
-    const int n = cg * R * R;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const int c = i / (R * R), r = i - c * R * R, ry = r / R, rx = r - ry * R;
-        int u1 = ox + rx, u2 = oy + ry;
-        u1 += (u1 < 0) ? G1 : 0;
-        u1 -= (u1 >= G1) ? G1 : 0;
+    // wrapped rows: one warp per (coil, row), lanes along the row
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    for (int cr = warp; cr < cg * R; cr += nwarp) {
+        const int c = cr / R, ry = cr - c * R;
+        int u2 = oy + ry;
         u2 += (u2 < 0) ? G2 : 0;
         u2 -= (u2 >= G2) ? G2 : 0;
-        float2 v = make_float2(0.f, 0.f);
-        if (c0 + c < nb) v = grid[u1 + (long long)G1 * (u2 + (long long)G2 * (c0 + c))];
-        reg[i] = v;
+        const bool cv = c0 + c < nb;
+        const float2* src = grid + (long long)G1 * (u2 + (long long)G2 * (c0 + c));
+        float2* dst = reg + (size_t)cr * R;
+        for (int rx = lane; rx < R; rx += 32) {
+            int u1 = ox + rx;
+            u1 += (u1 < 0) ? G1 : 0;
+            u1 -= (u1 >= G1) ? G1 : 0;
+            dst[rx] = cv ? src[u1] : make_float2(0.f, 0.f);
+        }
     }
     __syncthreads();
     return true;
@@ -430,7 +435,7 @@ struct Bin2DArgs {
     const float* wts;        // [M][2][W]
     const float* wfac;       // per-sample weight or null
     long long wfac_bstride;  // 0 or M
-    int G1, G2, T, ntx;
+    int G1, G2, T, lgT, ntx;
     long long M, nb;
     int cg;
     int use_tma;
@@ -497,17 +502,31 @@ __global__ void __launch_bounds__(256) interp2d_binned(const float2* __restrict_
 // Writes a CTA's accumulated tile: plain stores when the tile is owned by this
 // CTA, vector reductions of the non-zero cells into a pre-zeroed region when
 // several items share the tile.
+// Two cells per thread-iteration (float4); T is a power of two, te1 is even.
 __device__ __forceinline__ void flush_tile(const float2* acc, float2* __restrict__ out, bool heavy, int T, int u0,
                                            int v0, int te1, int te2, int c0, const Bin2DArgs& a) {
-    for (int i = threadIdx.x; i < a.cg * T * T; i += blockDim.x) {
-        const int c = i / (T * T), r = i - c * T * T, l2 = r / T, l1 = r - l2 * T;
+    const int lgT = a.lgT;
+    const int n2 = (a.cg << (2 * lgT)) >> 1;
+    const float4* acc4 = reinterpret_cast<const float4*>(acc);
+    for (int h = threadIdx.x; h < n2; h += blockDim.x) {
+        const int i = h << 1;
+        const int c = i >> (2 * lgT), r = i & ((1 << (2 * lgT)) - 1), l2 = r >> lgT, l1 = r & (T - 1);
         if (l1 < te1 && l2 < te2 && c0 + c < a.nb) {
             float2* d = out + (u0 + l1) + (long long)a.G1 * ((v0 + l2) + (long long)a.G2 * (c0 + c));
-            const float2 v = acc[i];
-            if (!heavy) *d = v;
-            else if (v.x != 0.f || v.y != 0.f) atomicAdd(d, v);
+            const float4 v = acc4[h];
+            if (!heavy) {
+                *reinterpret_cast<float4*>(d) = v;
+            } else {
+                if (v.x != 0.f || v.y != 0.f) atomicAdd(d, make_float2(v.x, v.y));
+                if (v.z != 0.f || v.w != 0.f) atomicAdd(d + 1, make_float2(v.z, v.w));
+            }
         }
     }
+}
+
+__device__ __forceinline__ void zero_acc(float2* acc, int n) {
+    float4* a4 = reinterpret_cast<float4*>(acc);
+    for (int h = threadIdx.x; h < (n >> 1); h += blockDim.x) a4[h] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
 // Zeroes the output regions of the heavy tiles: block (k, c) clears tile tiles[k] of plane c.
@@ -538,7 +557,7 @@ __global__ void __launch_bounds__(256) spread2d_binned(const float2* __restrict_
     const int tx = tile % a.ntx, ty = tile / a.ntx;
     const int u0 = tx * T, v0 = ty * T;
     const int te1 = min(T, a.G1 - u0), te2 = min(T, a.G2 - v0);
-    for (int i = threadIdx.x; i < a.cg * T * T; i += blockDim.x) acc[i] = make_float2(0.f, 0.f);
+    zero_acc(acc, a.cg * T * T);
     __syncthreads();
     const int e0 = item.y, e1 = item.z;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
@@ -598,7 +617,7 @@ __global__ void __launch_bounds__(256) gridnorm2d_binned(const float2* __restric
     const int tx = tile % a.ntx, ty = tile / a.ntx;
     const int u0 = tx * T, v0 = ty * T;
     const int te1 = min(T, a.G1 - u0), te2 = min(T, a.G2 - v0);
-    for (int i = threadIdx.x; i < a.cg * T * T; i += blockDim.x) acc[i] = make_float2(0.f, 0.f);
+    zero_acc(acc, a.cg * T * T);
     const int e0 = item.y, e1 = item.z;
     mbar_init(bar);
     if (e1 > e0) {
@@ -770,6 +789,8 @@ static Bin2DArgs bin_args(const NufftPlan& p, bool own, const float* wfac, long 
     a.G1 = p.G[0];
     a.G2 = p.G[1];
     a.T = b.T;
+    a.lgT = 0;
+    while ((1 << a.lgT) < b.T) ++a.lgT;
     a.ntx = b.ntx;
     a.M = p.M;
     a.nb = nb;

@@ -179,6 +179,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--ncu", action="store_true",
                     help="profiling mode: one warm-up solve, then one solve; prints nothing else")
     args = ap.parse_args()
@@ -200,6 +201,10 @@ def main():
     S = mm.nufftOp([N_IMG, N_IMG], case["kloc"], None, 1, 2.0, 4)
     R = mm.rcvrOp(case["maps"], 0)
     A = mm.mrSampOp(S, R)
+    tuned = None
+    if not args.no_autotune:
+        from matmri_gb300.autotune import autotune
+        tuned = autotune(A, use_cache=False)           # plan-time search, outside the timed region
     data = A(case["img"], "notransp")                 # synthetic k-space [M, C] (set-up, not timed)
     M = data.shape[0]
     dev = torch.device("cuda", local)
@@ -287,7 +292,7 @@ def main():
     cnt = (C.c_int32 * 5)()
     reps = 20
     _lib.check(lib.mmr_sense_profile_normal(A.handle, p.data_ptr(), q.data_ptr(), reps, ms, cnt, sp))
-    cc, tile, cgrp, item = A.get_tuning()
+    cc, tile, cgrp, item, flines = A.get_tuning()
     G = S.osN[0]
     sb = stage_bytes(cc, N_IMG, G, M, 4)
     total_ms = sum(ms[i] for i in range(5))
@@ -306,9 +311,9 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "c64 (FP64 CG scalars)", "data": "synthetic",
             "config": {"workload": WORKLOAD, "image": [N_IMG, N_IMG], "coils": N_COIL, "samples": M,
                        "iterations": NIT, "coil_chunk": cc, "tile": tile, "coil_group": cgrp,
-                       "item": item, "grid": [G, G],
+                       "item": item, "fft_lines": flines, "grid": [G, G],
                        "l2": "flushed between timed steps (512 MiB write, outside the per-step events)",
-                       "parallelism": f"replicas x{ws}"},
+                       "parallelism": f"replicas x{ws}", "autotuned": tuned is not None},
             "e2e": {"value": ws * args.steps / t_e2e, "unit": "solves/s",
                     "h2d_bytes_per_step": int(M * N_COIL * 8), "d2h_bytes_per_step": int(N_IMG * N_IMG * 8)},
             "gpu_launches": launches,

@@ -625,44 +625,65 @@ __global__ void __launch_bounds__(256) gridnorm2d_binned(const float2* __restric
     }
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-    const int grp = lane / TM::LPP, gl = lane % TM::LPP;
     constexpr int off0 = -W / 2 + 1;
-    // warp per entry: decode the taps once (region offsets, accumulator offsets,
-    // weights), then interp -> weight -> spread for every coil of the group
+    float2* sval = acc + (size_t)a.cg * T * T;          // interpolated, weighted samples [entry][coil]
+    int lgcg = 0;
+    while ((1 << lgcg) < a.cg) ++lgcg;
+    // phase 1 — interpolation, one thread per (entry, coil), separable weights:
+    //   v = sum_b w2[b] sum_a w1[a] g[b][a]; independent loads, no shuffles, no atomics
+    const int npair = (e1 - e0) << lgcg;
+    for (int p = threadIdx.x; p < npair; p += blockDim.x) {
+        const int e = e0 + (p >> lgcg), c = p & (a.cg - 1);
+        const int s = a.ent_s[e];
+        const short2 lb = a.ent_lb[e];
+        const float* w = a.wts + (size_t)s * 2 * W;
+        float w1[W], w2[W];
+#pragma unroll
+        for (int i = 0; i < W; ++i) {
+            w1[i] = w[i];
+            w2[i] = w[W + i];
+        }
+        const float2* rc = reg + (size_t)c * R * R + (lb.y + off0 + W) * R + (lb.x + off0 + W);
+        float2 v = make_float2(0.f, 0.f);
+#pragma unroll
+        for (int b = 0; b < W; ++b) {
+            float2 row = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int q = 0; q < W; ++q) {
+                const float2 g = rc[b * R + q];
+                row.x += w1[q] * g.x;
+                row.y += w1[q] * g.y;
+            }
+            v.x += w2[b] * row.x;
+            v.y += w2[b] * row.y;
+        }
+        float f = 1.f;
+        if (a.wfac && c0 + c < a.nb) f = a.wfac[s + a.wfac_bstride * (c0 + c)];
+        sval[p] = make_float2(v.x * f, v.y * f);
+    }
+    __syncthreads();
+    // phase 2 — spreading, one lane per tap; the entry's taps are decoded once per warp
+    const int grp = lane / TM::LPP, gl = lane % TM::LPP;
     for (int e = e0 + warp; e < e1; e += nwarp) {
         const int s = a.ent_s[e];
         const short2 lb = a.ent_lb[e];
         const float* w = a.wts + (size_t)s * 2 * W;
         float wt[TM::TPL];
-        int ro[TM::TPL], ao[TM::TPL];
+        int ao[TM::TPL];
 #pragma unroll
         for (int i = 0; i < TM::TPL; ++i) {
             const int k = gl + i * TM::LPP;
             const int ta = k % W, tb = k / W;
-            const bool ok = k < TM::TAPS;
             const int l1 = lb.x + off0 + ta, l2 = lb.y + off0 + tb;
+            const bool ok = k < TM::TAPS && l1 >= 0 && l1 < te1 && l2 >= 0 && l2 < te2;
             wt[i] = ok ? w[ta] * w[W + tb] : 0.f;
-            ro[i] = ok ? (l2 + W) * R + (l1 + W) : 0;
-            ao[i] = (ok && l1 >= 0 && l1 < te1 && l2 >= 0 && l2 < te2) ? l2 * T + l1 : -1;
+            ao[i] = ok ? l2 * T + l1 : -1;
         }
+        const float2* sv = sval + ((e - e0) << lgcg);
         for (int cb = 0; cb < a.cg; cb += TM::PPW) {
             const int c = cb + grp;
-            const bool cv = c < a.cg && c0 + c < a.nb;
-            const float2* rc = reg + (size_t)(c < a.cg ? c : 0) * R * R;
-            float2 v = make_float2(0.f, 0.f);
-#pragma unroll
-            for (int i = 0; i < TM::TPL; ++i) {
-                const float2 g = rc[ro[i]];
-                v.x += wt[i] * g.x;
-                v.y += wt[i] * g.y;
-            }
-            v = group_sum<TM::LPP>(v);
-            if (!cv) continue;
-            if (a.wfac) {
-                const float f = a.wfac[s + a.wfac_bstride * (c0 + c)];
-                v.x *= f;
-                v.y *= f;
-            }
+            if (c >= a.cg || c0 + c >= a.nb) continue;
+            const float2 v = sv[c];
             float2* ac = acc + (size_t)c * T * T;
 #pragma unroll
             for (int i = 0; i < TM::TPL; ++i) {
@@ -896,7 +917,7 @@ void nufft_grid_normal(NufftPlan& p, const float2* gin, float2* gout, long long 
                        cudaStream_t st, const int* active) {
     MMR_REQUIRE(p.use_bins, "fused gridding needs the 2D binned path");
     const int T = p.bins.T, R = T + 2 * p.W;
-    const int cg = pick_cg(p, nb, (size_t)(R * R + T * T) * 8, kTmaSmemExtra);
+    const int cg = pick_cg(p, nb, (size_t)(R * R + T * T + p.bins.chunk) * 8, kTmaSmemExtra);
     static const void* cptr = nullptr;
     static long long cnb = 0;
     static int ccg = 0, cR = 0, cG1 = 0, cG2 = 0;
@@ -909,7 +930,7 @@ void nufft_grid_normal(NufftPlan& p, const float2* gin, float2* gout, long long 
         cG1 = p.G[0];
         cG2 = p.G[1];
     }
-    const size_t smem = kTmaSmemExtra + (size_t)cg * (R * R + T * T) * 8;
+    const size_t smem = kTmaSmemExtra + (size_t)cg * (R * R + T * T + p.bins.chunk) * 8;
     Bin2DArgs a = bin_args(p, false, wfac, wfb, nb, cg, true, active);
     dim3 gridDim((unsigned)p.bins.n_pad_items, (unsigned)cdiv(nb, cg));
     zero_heavy(p, gout, nb, st, active);

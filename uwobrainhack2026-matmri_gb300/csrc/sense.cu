@@ -410,10 +410,13 @@ extern "C" int mmr_sense_set_tuning(mmr_sense* h, const mmr_tuning* t) {
         MMR_REQUIRE(t->coil_group == 0 || t->coil_group == 1 || t->coil_group == 2 || t->coil_group == 4 ||
                         t->coil_group == 8, "coil_group must be 1, 2, 4 or 8");
         MMR_REQUIRE(t->item == 0 || t->item >= 8, "item must be >= 8");
+        MMR_REQUIRE(t->fft_lines == 0 || (t->fft_lines >= 1 && t->fft_lines <= 16 && (t->fft_lines & (t->fft_lines - 1)) == 0),
+                    "fft_lines must be a power of two in 1..16");
         if (t->coil_chunk > 0) a.coil_chunk = t->coil_chunk;
         if (a.nufft) {
             NufftPlan& p = *a.nufft;
             if (t->coil_group > 0) p.cg_pref = t->coil_group;
+            if (t->fft_lines > 0) p.fft_lines = t->fft_lines;
             const int tile = t->tile > 0 ? t->tile : p.bins.T;
             const int item = t->item > 0 ? t->item : p.bins.chunk;
             if (p.nd == 2 && (tile != p.bins.T || item != p.bins.chunk)) {
@@ -434,6 +437,7 @@ extern "C" int mmr_sense_get_tuning(const mmr_sense* h, mmr_tuning* t) {
         t->tile = a.nufft && a.nufft->use_bins ? a.nufft->bins.T : 0;
         t->coil_group = a.nufft ? a.nufft->cg_pref : 0;
         t->item = a.nufft && a.nufft->use_bins ? a.nufft->bins.chunk : 0;
+        t->fft_lines = a.nufft ? a.nufft->fft_lines : 0;
     });
 }
 

@@ -1,0 +1,104 @@
+"""Autotuner for the SENSE normal operator's launch shapes.
+
+Knobs (``mmr_tuning``): coils per pipeline pass (``coil_chunk``, the grids of
+one pass stay resident in L2), gridding tile side (``tile``), coils per CTA in
+the gridding kernels (``coil_group``), samples per gridding work item
+(``item``) and transform lines per CTA in the FFT passes (``fft_lines``).
+
+The search is a coordinate descent from the current setting: each knob in
+turn is swept over its candidates with the others fixed, for two rounds.
+Every candidate is timed with CUDA events around the normal operator
+(``mmr_sense_profile_normal``).  Results are cached per size class (image
+size, oversampled grid, samples, coils, kernel width) and device in a JSON
+file (``$MATMRI_GB300_TUNE_CACHE`` or ``~/.cache/matmri_gb300/tuning.json``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import os
+
+import numpy as np
+
+from . import _lib
+
+SPACE = {
+    "coil_chunk": [4, 8, 16],
+    "tile": [16, 32],
+    "coil_group": [2, 4, 8],
+    "item": [32, 64, 128, 256],
+    "fft_lines": [4, 8, 16],
+}
+ORDER = ["item", "coil_group", "tile", "fft_lines", "coil_chunk"]
+
+
+def _cache_path():
+    p = os.environ.get("MATMRI_GB300_TUNE_CACHE")
+    if p:
+        return p
+    return os.path.join(os.path.expanduser("~"), ".cache", "matmri_gb300", "tuning.json")
+
+
+def _device_key():
+    lib = _lib.load()
+    sm, smem, ma, mi = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+    _lib.check(lib.mmr_device_info(C.byref(sm), C.byref(smem), C.byref(ma), C.byref(mi)))
+    return f"sm{ma.value}{mi.value}x{sm.value}"
+
+
+def size_class(op) -> str:
+    S = op.S
+    osN = getattr(S, "osN", None)
+    kw = getattr(S, "kwidth", 0)
+    return f"N{'x'.join(map(str, op.imN))}_G{'x'.join(map(str, osN or []))}_M{op.M}_C{op.C}_W{kw}"
+
+
+def time_normal(op, x_ptr, y_ptr, reps=5) -> float:
+    """Mean ms of one normal operator application (sum over stages)."""
+    lib = _lib.load()
+    ms = (C.c_double * 5)()
+    cnt = (C.c_int32 * 5)()
+    _lib.check(lib.mmr_sense_profile_normal(op.handle, x_ptr, y_ptr, int(reps), ms, cnt, None))
+    return sum(ms[i] for i in range(5)) / reps
+
+
+def autotune(op, reps=5, rounds=2, use_cache=True, verbose=False) -> dict:
+    """Tunes ``op`` (an mrSampOp over a 2D nufftOp) in place; returns the chosen knobs."""
+    key = f"{_device_key()}/{size_class(op)}"
+    path = _cache_path()
+    cache = {}
+    if use_cache and os.path.exists(path):
+        try:
+            cache = json.load(open(path))
+        except Exception:
+            cache = {}
+    if use_cache and key in cache:
+        op.set_tuning(**cache[key]["tuning"])
+        return dict(cache[key]["tuning"])
+    import torch  # device buffers for the probe
+    n = int(np.prod(op.imN))
+    x = torch.randn(n, dtype=torch.complex64, device="cuda")
+    y = torch.empty_like(x)
+    cur = dict(zip(["coil_chunk", "tile", "coil_group", "item", "fft_lines"], op.get_tuning()))
+    best_t = time_normal(op, x.data_ptr(), y.data_ptr(), reps)
+    for _ in range(rounds):
+        for knob in ORDER:
+            for v in SPACE[knob]:
+                if v == cur[knob] or (knob == "coil_chunk" and v > op.C):
+                    continue
+                trial = dict(cur, **{knob: v})
+                op.set_tuning(**trial)
+                t = time_normal(op, x.data_ptr(), y.data_ptr(), reps)
+                if verbose:
+                    print(f"autotune {trial} -> {t:.4f} ms")
+                if t < best_t:
+                    best_t, cur = t, trial
+            op.set_tuning(**cur)
+    if use_cache:
+        cache[key] = {"tuning": cur, "normal_ms": best_t}
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        tmp = path + ".tmp"
+        with open(tmp, "w") as f:
+            json.dump(cache, f, indent=1)
+        os.replace(tmp, path)
+    return cur

@@ -14,18 +14,21 @@
 //    evaluates the W x W taps of a sample with one lane per tap and a
 //    warp-shuffle reduction;
 //  * spread2d_binned  — adjoint spreading; samples are pre-sorted into the
-//    tiles their footprint touches and split into work items of bounded size;
-//    each CTA accumulates its item in a shared-memory tile.  A tile served by
-//    one item is owned and flushed with coalesced plain stores (no memset);
-//    the few dense tiles (the centre of a variable-density trajectory) are
-//    zeroed first and their items add non-zero cells with vector reductions;
+//    tiles their footprint touches.  Tiles are adaptive (a quadtree): a
+//    32 x 32 tile holding more samples than one work item allows — the dense
+//    centre of a variable-density trajectory — is split into 16 x 16 and
+//    8 x 8 sub-tiles.  Every output cell is owned by exactly one CTA, which
+//    accumulates its (sub)tile in shared memory and flushes it with coalesced
+//    plain stores: no global atomics, no memset of the grid, deterministic;
 //  * gridnorm2d_binned — the two fused for the normal operator
-//    C^H diag(w) C: interp from a staged tile + 2W halo, weight, spread into
-//    the owned tile; the samples never round-trip through HBM;
+//    C^H diag(w) C: interp from a staged tile + 2W halo (one thread per
+//    sample and coil, separable weights), weight, spread into the owned tile
+//    (one lane per tap); the samples never round-trip through HBM;
 //  * interp_generic / spread_generic — any ndim / small grids.
 #include <algorithm>
 #include <cmath>
 #include <cudaTypedefs.h>
+#include <functional>
 
 #include "nufft.cuh"
 
@@ -184,31 +187,14 @@ void nufft_set_dcf(NufftPlan& p, const double* dcf) {
     p.has_dcf = true;
 }
 
-// Splits every tile's entry range [ptr[t], ptr[t+1]) into items of <= chunk entries.
-static void make_items(const std::vector<int>& ptr, int chunk, std::vector<int4>& items, std::vector<int>* heavy) {
-    items.clear();
-    if (heavy) heavy->clear();
-    const int ntile = (int)ptr.size() - 1;
-    for (int t = 0; t < ntile; ++t) {
-        const int n = ptr[t + 1] - ptr[t];
-        const int nit = (n + chunk - 1) / chunk;
-        const int hv = nit > 1 ? 1 : 0;
-        if (hv && heavy) heavy->push_back(t);
-        if (n == 0 && heavy) {   // empty tiles still own (and zero) their output region
-            items.push_back(make_int4(t, ptr[t], ptr[t], 0));
-            continue;
-        }
-        for (int k = 0; k < nit; ++k) {
-            const int e0 = ptr[t] + k * chunk, e1 = std::min(ptr[t + 1], e0 + chunk);
-            items.push_back(make_int4(t, e0, e1, hv));
-        }
-    }
-}
+// Work item encoding: {u0 | v0 << 16, e0, e1, tile side}.
+static inline int4 item_of(int u0, int v0, int e0, int e1, int T) { return make_int4(u0 | (v0 << 16), e0, e1, T); }
 
 void nufft_build_bins(NufftPlan& p, int Treq, int chunk) {
     p.use_bins = false;
     if (p.nd != 2) return;
     MMR_REQUIRE(chunk >= 8, "work-item chunk must be >= 8");
+    MMR_REQUIRE(p.G[0] < 65536 && p.G[1] < 65536, "grid too large for the binned path");
     p.bins.chunk = chunk;
     int T = Treq;
     while (T >= 8 && (p.G[0] < 2 * (T + 2 * p.W) || p.G[1] < 2 * (T + 2 * p.W))) T /= 2;
@@ -225,7 +211,8 @@ void nufft_build_bins(NufftPlan& p, int Treq, int chunk) {
         long long r = imod(a, g);
         return (int)(r >= g / 2 ? r - g : r);
     };
-    // own lists
+    // ---- own lists (interpolation): each sample once, in the tile holding its base cell,
+    //      split into items of <= chunk samples (no output conflicts)
     std::vector<int> cnt(ntile + 1, 0);
     for (long long s = 0; s < p.M; ++s) {
         const int c1 = base[s], c2 = base[p.M + s];
@@ -243,56 +230,78 @@ void nufft_build_bins(NufftPlan& p, int Treq, int chunk) {
         own_s[e] = (int)s;
         own_lb[e] = make_short2((short)(c1 - tx * T), (short)(c2 - ty * T));
     }
-    b.own_ptr.upload(cnt);
+    std::vector<int4> items;
+    for (int t = 0; t < ntile; ++t) {
+        const int u0 = (t % b.ntx) * T, v0 = (t / b.ntx) * T;
+        for (int e0 = cnt[t]; e0 < cnt[t + 1]; e0 += chunk)
+            items.push_back(item_of(u0, v0, e0, std::min(cnt[t + 1], e0 + chunk), T));
+    }
     b.own_s.upload(own_s);
     b.own_lb.upload(own_lb);
+    b.own_items.upload(items);
+    b.n_own_items = (int)items.size();
     b.n_own = p.M;
-    // padded lists: every tile touched by the footprint
+    // ---- padded lists (spreading / fused normal op): every output tile owns its cells and
+    //      lists every sample whose footprint touches it.  Tiles holding more than `chunk`
+    //      samples (the dense centre of a variable-density trajectory) are split into
+    //      quadrants down to 8 x 8 cells, so that work stays balanced without atomics.
     std::vector<std::vector<int>> tiles_s(ntile);
-    std::vector<std::vector<short2>> tiles_lb(ntile);
     for (long long s = 0; s < p.M; ++s) {
         const int c[2] = {base[s], base[p.M + s]};
         int tl[2][8], ntl[2] = {0, 0};
         for (int k = 0; k < 2; ++k) {
             for (int j = 0; j < p.W; ++j) {
-                const int u = (int)imod(c[k] + off0 + j, p.G[k]);
-                const int ti = u / T;
+                const int ti = (int)imod(c[k] + off0 + j, p.G[k]) / T;
                 bool seen = false;
                 for (int q = 0; q < ntl[k]; ++q) seen |= (tl[k][q] == ti);
                 if (!seen) tl[k][ntl[k]++] = ti;
             }
         }
         for (int a = 0; a < ntl[0]; ++a)
-            for (int bb = 0; bb < ntl[1]; ++bb) {
-                const int tx = tl[0][a], ty = tl[1][bb], t = ty * b.ntx + tx;
-                tiles_s[t].push_back((int)s);
-                tiles_lb[t].push_back(make_short2((short)sdist((long long)c[0] - (long long)tx * T, p.G[0]),
-                                                  (short)sdist((long long)c[1] - (long long)ty * T, p.G[1])));
-            }
+            for (int bb = 0; bb < ntl[1]; ++bb) tiles_s[tl[1][bb] * b.ntx + tl[0][a]].push_back((int)s);
     }
-    std::vector<int> pptr(ntile + 1, 0), ps;
+    auto touches = [&](int s, int u0, int v0, int Tt) {
+        const int c[2] = {base[s], base[p.M + s]}, o[2] = {u0, v0};
+        for (int k = 0; k < 2; ++k) {
+            bool hit = false;
+            for (int j = 0; j < p.W && !hit; ++j) hit = imod((long long)c[k] + off0 + j - o[k], p.G[k]) < Tt;
+            if (!hit) return false;
+        }
+        return true;
+    };
+    std::vector<int> ps;
     std::vector<short2> plb;
+    items.clear();
     b.max_pad = 0;
-    for (int t = 0; t < ntile; ++t) {
-        pptr[t + 1] = pptr[t] + (int)tiles_s[t].size();
-        b.max_pad = std::max(b.max_pad, (int)tiles_s[t].size());
-        ps.insert(ps.end(), tiles_s[t].begin(), tiles_s[t].end());
-        plb.insert(plb.end(), tiles_lb[t].begin(), tiles_lb[t].end());
-    }
-    b.pad_ptr.upload(pptr);
+    std::function<void(int, int, int, const std::vector<int>&)> split = [&](int u0, int v0, int Tt,
+                                                                             const std::vector<int>& list) {
+        if (u0 >= p.G[0] || v0 >= p.G[1]) return;
+        if ((int)list.size() > chunk && Tt > 8) {
+            const int h = Tt / 2;
+            for (int dv = 0; dv < 2; ++dv)
+                for (int du = 0; du < 2; ++du) {
+                    std::vector<int> sub;
+                    for (int s : list)
+                        if (touches(s, u0 + du * h, v0 + dv * h, h)) sub.push_back(s);
+                    split(u0 + du * h, v0 + dv * h, h, sub);
+                }
+            return;
+        }
+        const int e0 = (int)ps.size();
+        for (int s : list) {
+            ps.push_back(s);
+            plb.push_back(make_short2((short)sdist((long long)base[s] - u0, p.G[0]),
+                                      (short)sdist((long long)base[p.M + s] - v0, p.G[1])));
+        }
+        b.max_pad = std::max(b.max_pad, (int)list.size());
+        items.push_back(item_of(u0, v0, e0, (int)ps.size(), Tt));   // empty tiles still write zeros
+    };
+    for (int t = 0; t < ntile; ++t) split((t % b.ntx) * T, (t / b.ntx) * T, T, tiles_s[t]);
     b.pad_s.upload(ps);
     b.pad_lb.upload(plb);
     b.n_pad = (long long)ps.size();
-    std::vector<int4> items;
-    std::vector<int> heavy;
-    make_items(cnt, chunk, items, nullptr);
-    b.own_items.upload(items);
-    b.n_own_items = (int)items.size();
-    make_items(pptr, chunk, items, &heavy);
     b.pad_items.upload(items);
     b.n_pad_items = (int)items.size();
-    b.heavy.upload(heavy);
-    b.n_heavy = (int)heavy.size();
     p.use_bins = true;
     p.tmap_ptr = nullptr;   // invalidate descriptor caches (box depends on T)
 }
@@ -429,7 +438,7 @@ __device__ __forceinline__ float2 group_sum(float2 v) {
 
 // ------------------------------------------------------- binned 2D kernels ----
 struct Bin2DArgs {
-    const int4* items;       // {tile, e0, e1, heavy}
+    const int4* items;       // {u0 | v0 << 16, e0, e1, tile side}
     const int* ent_s;
     const short2* ent_lb;
     const float* wts;        // [M][2][W]
@@ -439,6 +448,7 @@ struct Bin2DArgs {
     long long M, nb;
     int cg;
     int use_tma;
+    int chunk;               // max entries per phase batch (sval capacity)
     const int* active;
 };
 
@@ -452,14 +462,12 @@ __global__ void __launch_bounds__(256) interp2d_binned(const float2* __restrict_
     uint64_t* bar;
     float2* reg = tma_layout(sm4, &bar);
     const int4 item = a.items[blockIdx.x];
-    const int tile = item.x;
+    const int u0 = item.x & 0xffff, v0 = item.x >> 16;
     const int c0 = blockIdx.y * a.cg;
     const int e0 = item.y, e1 = item.z;
     if (e0 == e1) return;
-    const int tx = tile % a.ntx, ty = tile / a.ntx;
     mbar_init(bar);
-    if (!stage_region(reg, grid, &tmap, a.use_tma, bar, tx * a.T - W / 2, ty * a.T - W / 2, c0, a.cg, R, a.G1, a.G2,
-                      a.nb))
+    if (!stage_region(reg, grid, &tmap, a.use_tma, bar, u0 - W / 2, v0 - W / 2, c0, a.cg, R, a.G1, a.G2, a.nb))
         return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
     const int grp = lane / TM::LPP, gl = lane % TM::LPP;
@@ -503,9 +511,9 @@ __global__ void __launch_bounds__(256) interp2d_binned(const float2* __restrict_
 // CTA, vector reductions of the non-zero cells into a pre-zeroed region when
 // several items share the tile.
 // Two cells per thread-iteration (float4); T is a power of two, te1 is even.
-__device__ __forceinline__ void flush_tile(const float2* acc, float2* __restrict__ out, bool heavy, int T, int u0,
-                                           int v0, int te1, int te2, int c0, const Bin2DArgs& a) {
-    const int lgT = a.lgT;
+__device__ __forceinline__ void flush_tile(const float2* acc, float2* __restrict__ out, int T, int u0, int v0, int te1,
+                                           int te2, int c0, const Bin2DArgs& a) {
+    const int lgT = 31 - __clz(T);
     const int n2 = (a.cg << (2 * lgT)) >> 1;
     const float4* acc4 = reinterpret_cast<const float4*>(acc);
     for (int h = threadIdx.x; h < n2; h += blockDim.x) {
@@ -513,13 +521,7 @@ __device__ __forceinline__ void flush_tile(const float2* acc, float2* __restrict
         const int c = i >> (2 * lgT), r = i & ((1 << (2 * lgT)) - 1), l2 = r >> lgT, l1 = r & (T - 1);
         if (l1 < te1 && l2 < te2 && c0 + c < a.nb) {
             float2* d = out + (u0 + l1) + (long long)a.G1 * ((v0 + l2) + (long long)a.G2 * (c0 + c));
-            const float4 v = acc4[h];
-            if (!heavy) {
-                *reinterpret_cast<float4*>(d) = v;
-            } else {
-                if (v.x != 0.f || v.y != 0.f) atomicAdd(d, make_float2(v.x, v.y));
-                if (v.z != 0.f || v.w != 0.f) atomicAdd(d + 1, make_float2(v.z, v.w));
-            }
+            *reinterpret_cast<float4*>(d) = acc4[h];
         }
     }
 }
@@ -529,20 +531,6 @@ __device__ __forceinline__ void zero_acc(float2* acc, int n) {
     for (int h = threadIdx.x; h < (n >> 1); h += blockDim.x) a4[h] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
-// Zeroes the output regions of the heavy tiles: block (k, c) clears tile tiles[k] of plane c.
-__global__ void __launch_bounds__(256) zero_tiles_kernel(float2* __restrict__ out, const int* __restrict__ tiles,
-                                                         int T, int ntx, int G1, int G2, const int* active) {
-    if (active && *active) return;
-    const int t = tiles[blockIdx.x];
-    const int u0 = (t % ntx) * T, v0 = (t / ntx) * T;
-    const int te1 = min(T, G1 - u0), te2 = min(T, G2 - v0);
-    float2* o = out + (long long)G1 * G2 * blockIdx.y;
-    for (int i = threadIdx.x; i < T * T; i += blockDim.x) {
-        const int l2 = i / T, l1 = i - l2 * T;
-        if (l1 < te1 && l2 < te2) o[(u0 + l1) + (long long)G1 * (v0 + l2)] = make_float2(0.f, 0.f);
-    }
-}
-
 template <int W>
 __global__ void __launch_bounds__(256) spread2d_binned(const float2* __restrict__ y, float2* __restrict__ grid,
                                                        const Bin2DArgs a) {
@@ -550,12 +538,10 @@ __global__ void __launch_bounds__(256) spread2d_binned(const float2* __restrict_
     extern __shared__ float4 sm4[];
     if (a.active && *a.active) return;
     float2* acc = reinterpret_cast<float2*>(sm4);
-    const int T = a.T;
     const int4 item = a.items[blockIdx.x];
-    const int tile = item.x;
+    const int T = item.w;                      // this item's (sub)tile side
+    const int u0 = item.x & 0xffff, v0 = item.x >> 16;
     const int c0 = blockIdx.y * a.cg;
-    const int tx = tile % a.ntx, ty = tile / a.ntx;
-    const int u0 = tx * T, v0 = ty * T;
     const int te1 = min(T, a.G1 - u0), te2 = min(T, a.G2 - v0);
     zero_acc(acc, a.cg * T * T);
     __syncthreads();
@@ -598,7 +584,7 @@ __global__ void __launch_bounds__(256) spread2d_binned(const float2* __restrict_
         }
     }
     __syncthreads();
-    flush_tile(acc, grid, item.w != 0, T, u0, v0, te1, te2, c0, a);
+    flush_tile(acc, grid, T, u0, v0, te1, te2, c0, a);
 }
 
 template <int W>
@@ -607,33 +593,38 @@ __global__ void __launch_bounds__(256) gridnorm2d_binned(const float2* __restric
     using TM = TapMap<W>;
     extern __shared__ float4 sm4[];
     if (a.active && *a.active) return;
-    const int T = a.T, R = T + 2 * W;
+    const int R0 = a.T + 2 * W;                // region side of a full tile (smem layout)
     uint64_t* bar;
     float2* reg = tma_layout(sm4, &bar);
-    float2* acc = reg + (size_t)a.cg * R * R;
+    float2* acc = reg + (size_t)a.cg * R0 * R0;
     const int4 item = a.items[blockIdx.x];
-    const int tile = item.x;
+    const int T = item.w, R = T + 2 * W;       // this item's (sub)tile and region sides
+    const int u0 = item.x & 0xffff, v0 = item.x >> 16;
     const int c0 = blockIdx.y * a.cg;
-    const int tx = tile % a.ntx, ty = tile / a.ntx;
-    const int u0 = tx * T, v0 = ty * T;
     const int te1 = min(T, a.G1 - u0), te2 = min(T, a.G2 - v0);
     zero_acc(acc, a.cg * T * T);
     const int e0 = item.y, e1 = item.z;
     mbar_init(bar);
     if (e1 > e0) {
-        if (!stage_region(reg, gin, &tmap, a.use_tma, bar, u0 - W, v0 - W, c0, a.cg, R, a.G1, a.G2, a.nb)) return;
+        // the tensor map's box is a full tile's region: sub-tiles use plain loads
+        if (!stage_region(reg, gin, &tmap, a.use_tma && T == a.T, bar, u0 - W, v0 - W, c0, a.cg, R, a.G1, a.G2,
+                          a.nb))
+            return;
     }
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
     constexpr int off0 = -W / 2 + 1;
-    float2* sval = acc + (size_t)a.cg * T * T;          // interpolated, weighted samples [entry][coil]
+    float2* sval = acc + (size_t)a.cg * a.T * a.T;      // interpolated, weighted samples [entry][coil]
     int lgcg = 0;
     while ((1 << lgcg) < a.cg) ++lgcg;
+    // entries are processed in batches of a.chunk (the capacity of sval)
+    for (int eb = e0; eb < e1; eb += a.chunk) {
+    const int ee = min(e1, eb + a.chunk);
     // phase 1 — interpolation, one thread per (entry, coil), separable weights:
     //   v = sum_b w2[b] sum_a w1[a] g[b][a]; independent loads, no shuffles, no atomics
-    const int npair = (e1 - e0) << lgcg;
+    const int npair = (ee - eb) << lgcg;
     for (int p = threadIdx.x; p < npair; p += blockDim.x) {
-        const int e = e0 + (p >> lgcg), c = p & (a.cg - 1);
+        const int e = eb + (p >> lgcg), c = p & (a.cg - 1);
         const int s = a.ent_s[e];
         const short2 lb = a.ent_lb[e];
         const float* w = a.wts + (size_t)s * 2 * W;
@@ -664,7 +655,7 @@ __global__ void __launch_bounds__(256) gridnorm2d_binned(const float2* __restric
     __syncthreads();
     // phase 2 — spreading, one lane per tap; the entry's taps are decoded once per warp
     const int grp = lane / TM::LPP, gl = lane % TM::LPP;
-    for (int e = e0 + warp; e < e1; e += nwarp) {
+    for (int e = eb + warp; e < ee; e += nwarp) {
         const int s = a.ent_s[e];
         const short2 lb = a.ent_lb[e];
         const float* w = a.wts + (size_t)s * 2 * W;
@@ -679,7 +670,7 @@ __global__ void __launch_bounds__(256) gridnorm2d_binned(const float2* __restric
             wt[i] = ok ? w[ta] * w[W + tb] : 0.f;
             ao[i] = ok ? l2 * T + l1 : -1;
         }
-        const float2* sv = sval + ((e - e0) << lgcg);
+        const float2* sv = sval + ((e - eb) << lgcg);
         for (int cb = 0; cb < a.cg; cb += TM::PPW) {
             const int c = cb + grp;
             if (c >= a.cg || c0 + c >= a.nb) continue;
@@ -695,7 +686,9 @@ __global__ void __launch_bounds__(256) gridnorm2d_binned(const float2* __restric
         }
     }
     __syncthreads();
-    flush_tile(acc, gout, item.w != 0, T, u0, v0, te1, te2, c0, a);
+    }
+    __syncthreads();
+    flush_tile(acc, gout, T, u0, v0, te1, te2, c0, a);
 }
 
 // ------------------------------------------------------------ generic kernels --
@@ -817,6 +810,7 @@ static Bin2DArgs bin_args(const NufftPlan& p, bool own, const float* wfac, long 
     a.nb = nb;
     a.cg = cg;
     a.use_tma = tma ? 1 : 0;
+    a.chunk = b.chunk;
     a.active = active;
     return a;
 }
@@ -879,14 +873,6 @@ void nufft_interp(NufftPlan& p, const float2* grid, float2* y, long long nb, con
     check_launch("interp2d_binned");
 }
 
-static void zero_heavy(NufftPlan& p, float2* out, long long nb, cudaStream_t st, const int* active) {
-    const BinLists& b = p.bins;
-    if (b.n_heavy == 0) return;
-    zero_tiles_kernel<<<dim3((unsigned)b.n_heavy, (unsigned)nb), 256, 0, st>>>(out, b.heavy.as<int>(), b.T, b.ntx,
-                                                                           p.G[0], p.G[1], active);
-    check_launch("zero_tiles");
-}
-
 void nufft_spread(NufftPlan& p, const float2* y, float2* grid, long long nb, const float* wfac, long long wfb,
                   cudaStream_t st, const int* active) {
     if (!p.use_bins) {
@@ -901,7 +887,6 @@ void nufft_spread(NufftPlan& p, const float2* y, float2* grid, long long nb, con
     const size_t smem = (size_t)cg * T * T * 8;
     Bin2DArgs a = bin_args(p, false, wfac, wfb, nb, cg, false, active);
     dim3 gridDim((unsigned)p.bins.n_pad_items, (unsigned)cdiv(nb, cg));
-    zero_heavy(p, grid, nb, st, active);
     MMR_W_DISPATCH(p.W, {
         set_smem(spread2d_binned<KW>, smem);
         spread2d_binned<KW><<<gridDim, 256, smem, st>>>(y, grid, a);
@@ -933,7 +918,6 @@ void nufft_grid_normal(NufftPlan& p, const float2* gin, float2* gout, long long 
     const size_t smem = kTmaSmemExtra + (size_t)cg * (R * R + T * T + p.bins.chunk) * 8;
     Bin2DArgs a = bin_args(p, false, wfac, wfb, nb, cg, true, active);
     dim3 gridDim((unsigned)p.bins.n_pad_items, (unsigned)cdiv(nb, cg));
-    zero_heavy(p, gout, nb, st, active);
     MMR_W_DISPATCH(p.W, {
         set_smem(gridnorm2d_binned<KW>, smem);
         gridnorm2d_binned<KW><<<gridDim, 256, smem, st>>>(gin, gout, a, g_norm_map);

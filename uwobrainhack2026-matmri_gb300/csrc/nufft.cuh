@@ -9,20 +9,18 @@ namespace mmr {
 
 // Binned sample lists for one tile size (2D fast path).
 //
-// Work is split into items of at most `chunk` entries so that the dense centre
-// of a variable-density trajectory is spread over many CTAs.  A tile whose
-// padded list needs several items is "heavy": its output region is zeroed
-// first and every item adds its non-zero cells with vector reductions; a
-// light tile (one item) owns its region and writes it with plain stores.
+// Work is split into items of about `chunk` entries so that the dense centre
+// of a variable-density trajectory is spread over many CTAs: interpolation
+// items are chunks of a tile's own samples; spreading items are quadtree
+// (sub)tiles of 32, 16 or 8 cells that each own their output cells.
 struct BinLists {
-    int T = 0;                 // tile side (grid cells)
-    int chunk = 0;             // max entries per work item
+    int T = 0;                 // full tile side (grid cells)
+    int chunk = 0;             // target entries per work item
     int ntx = 0, nty = 0;
-    DevBuf own_ptr, own_s, own_lb;   // interp: each sample once (tile containing its base cell)
-    DevBuf pad_ptr, pad_s, pad_lb;   // spread/normal: every tile its footprint touches
-    DevBuf own_items, pad_items;     // int4 {tile, e0, e1, heavy}
-    DevBuf heavy;                    // int: heavy tile ids
-    int n_own_items = 0, n_pad_items = 0, n_heavy = 0;
+    DevBuf own_s, own_lb;            // interp: each sample once (tile containing its base cell)
+    DevBuf pad_s, pad_lb;            // spread/normal: every (sub)tile its footprint touches
+    DevBuf own_items, pad_items;     // int4 {u0 | v0 << 16, e0, e1, tile side}
+    int n_own_items = 0, n_pad_items = 0;
     long long n_own = 0, n_pad = 0;
     int max_own = 0, max_pad = 0;
 };

@@ -271,6 +271,7 @@ void nufft_build_bins(NufftPlan& p, int Treq, int chunk) {
     };
     std::vector<int> ps;
     std::vector<short2> plb;
+    std::vector<int2> heavy;   // {u0 | v0 << 16, side} of leaf tiles shared by several items
     items.clear();
     b.max_pad = 0;
     std::function<void(int, int, int, const std::vector<int>&)> split = [&](int u0, int v0, int Tt,
@@ -294,9 +295,18 @@ void nufft_build_bins(NufftPlan& p, int Treq, int chunk) {
                                       (short)sdist((long long)base[p.M + s] - v0, p.G[1])));
         }
         b.max_pad = std::max(b.max_pad, (int)list.size());
-        items.push_back(item_of(u0, v0, e0, (int)ps.size(), Tt));   // empty tiles still write zeros
+        const int e1 = (int)ps.size();
+        if (e1 - e0 <= chunk) {
+            items.push_back(item_of(u0, v0, e0, e1, Tt));   // owned; empty tiles still write zeros
+        } else {
+            // an 8 x 8 leaf still denser than one item: zeroed first, then its chunks add
+            heavy.push_back(make_int2(u0 | (v0 << 16), Tt));
+            for (int c = e0; c < e1; c += chunk) items.push_back(item_of(u0, v0, c, std::min(e1, c + chunk), Tt | 256));
+        }
     };
     for (int t = 0; t < ntile; ++t) split((t % b.ntx) * T, (t / b.ntx) * T, T, tiles_s[t]);
+    b.heavy.upload(heavy);
+    b.n_heavy = (int)heavy.size();
     b.pad_s.upload(ps);
     b.pad_lb.upload(plb);
     b.n_pad = (long long)ps.size();
@@ -511,8 +521,10 @@ __global__ void __launch_bounds__(256) interp2d_binned(const float2* __restrict_
 // CTA, vector reductions of the non-zero cells into a pre-zeroed region when
 // several items share the tile.
 // Two cells per thread-iteration (float4); T is a power of two, te1 is even.
-__device__ __forceinline__ void flush_tile(const float2* acc, float2* __restrict__ out, int T, int u0, int v0, int te1,
-                                           int te2, int c0, const Bin2DArgs& a) {
+// Owned (sub)tiles are written with plain float4 stores; a leaf tile shared by
+// several items (pre-zeroed) receives vector reductions of its non-zero cells.
+__device__ __forceinline__ void flush_tile(const float2* acc, float2* __restrict__ out, bool shared, int T, int u0,
+                                           int v0, int te1, int te2, int c0, const Bin2DArgs& a) {
     const int lgT = 31 - __clz(T);
     const int n2 = (a.cg << (2 * lgT)) >> 1;
     const float4* acc4 = reinterpret_cast<const float4*>(acc);
@@ -521,9 +533,36 @@ __device__ __forceinline__ void flush_tile(const float2* acc, float2* __restrict
         const int c = i >> (2 * lgT), r = i & ((1 << (2 * lgT)) - 1), l2 = r >> lgT, l1 = r & (T - 1);
         if (l1 < te1 && l2 < te2 && c0 + c < a.nb) {
             float2* d = out + (u0 + l1) + (long long)a.G1 * ((v0 + l2) + (long long)a.G2 * (c0 + c));
-            *reinterpret_cast<float4*>(d) = acc4[h];
+            const float4 v = acc4[h];
+            if (!shared) {
+                *reinterpret_cast<float4*>(d) = v;
+            } else {
+                if (v.x != 0.f || v.y != 0.f) atomicAdd(d, make_float2(v.x, v.y));
+                if (v.z != 0.f || v.w != 0.f) atomicAdd(d + 1, make_float2(v.z, v.w));
+            }
         }
     }
+}
+
+// Zeroes the shared leaf tiles (block (k, c): tile k of plane c) before their items add into them.
+__global__ void __launch_bounds__(256) zero_shared_tiles(float2* __restrict__ out, const int2* __restrict__ tiles,
+                                                         int G1, int G2, const int* active) {
+    if (active && *active) return;
+    const int2 t = tiles[blockIdx.x];
+    const int u0 = t.x & 0xffff, v0 = t.x >> 16, T = t.y;
+    float2* o = out + (long long)G1 * G2 * blockIdx.y;
+    for (int i = threadIdx.x; i < T * T; i += blockDim.x) {
+        const int l2 = i / T, l1 = i - l2 * T;
+        if (u0 + l1 < G1 && v0 + l2 < G2) o[(u0 + l1) + (long long)G1 * (v0 + l2)] = make_float2(0.f, 0.f);
+    }
+}
+
+static void zero_shared(NufftPlan& p, float2* out, long long nb, cudaStream_t st, const int* active) {
+    const BinLists& b = p.bins;
+    if (b.n_heavy == 0) return;
+    zero_shared_tiles<<<dim3((unsigned)b.n_heavy, (unsigned)nb), 256, 0, st>>>(out, b.heavy.as<int2>(), p.G[0],
+                                                                             p.G[1], active);
+    check_launch("zero_shared_tiles");
 }
 
 __device__ __forceinline__ void zero_acc(float2* acc, int n) {
@@ -539,7 +578,8 @@ __global__ void __launch_bounds__(256) spread2d_binned(const float2* __restrict_
     if (a.active && *a.active) return;
     float2* acc = reinterpret_cast<float2*>(sm4);
     const int4 item = a.items[blockIdx.x];
-    const int T = item.w;                      // this item's (sub)tile side
+    const int T = item.w & 255;                // this item's (sub)tile side
+    const bool shared = (item.w >> 8) != 0;    // tile split across several items
     const int u0 = item.x & 0xffff, v0 = item.x >> 16;
     const int c0 = blockIdx.y * a.cg;
     const int te1 = min(T, a.G1 - u0), te2 = min(T, a.G2 - v0);
@@ -584,7 +624,7 @@ __global__ void __launch_bounds__(256) spread2d_binned(const float2* __restrict_
         }
     }
     __syncthreads();
-    flush_tile(acc, grid, T, u0, v0, te1, te2, c0, a);
+    flush_tile(acc, grid, shared, T, u0, v0, te1, te2, c0, a);
 }
 
 template <int W>
@@ -598,7 +638,8 @@ __global__ void __launch_bounds__(256) gridnorm2d_binned(const float2* __restric
     float2* reg = tma_layout(sm4, &bar);
     float2* acc = reg + (size_t)a.cg * R0 * R0;
     const int4 item = a.items[blockIdx.x];
-    const int T = item.w, R = T + 2 * W;       // this item's (sub)tile and region sides
+    const int T = item.w & 255, R = T + 2 * W; // this item's (sub)tile and region sides
+    const bool shared = (item.w >> 8) != 0;    // tile split across several items
     const int u0 = item.x & 0xffff, v0 = item.x >> 16;
     const int c0 = blockIdx.y * a.cg;
     const int te1 = min(T, a.G1 - u0), te2 = min(T, a.G2 - v0);
@@ -688,7 +729,7 @@ __global__ void __launch_bounds__(256) gridnorm2d_binned(const float2* __restric
     __syncthreads();
     }
     __syncthreads();
-    flush_tile(acc, gout, T, u0, v0, te1, te2, c0, a);
+    flush_tile(acc, gout, shared, T, u0, v0, te1, te2, c0, a);
 }
 
 // ------------------------------------------------------------ generic kernels --
@@ -887,6 +928,7 @@ void nufft_spread(NufftPlan& p, const float2* y, float2* grid, long long nb, con
     const size_t smem = (size_t)cg * T * T * 8;
     Bin2DArgs a = bin_args(p, false, wfac, wfb, nb, cg, false, active);
     dim3 gridDim((unsigned)p.bins.n_pad_items, (unsigned)cdiv(nb, cg));
+    zero_shared(p, grid, nb, st, active);
     MMR_W_DISPATCH(p.W, {
         set_smem(spread2d_binned<KW>, smem);
         spread2d_binned<KW><<<gridDim, 256, smem, st>>>(y, grid, a);
@@ -918,6 +960,7 @@ void nufft_grid_normal(NufftPlan& p, const float2* gin, float2* gout, long long 
     const size_t smem = kTmaSmemExtra + (size_t)cg * (R * R + T * T + p.bins.chunk) * 8;
     Bin2DArgs a = bin_args(p, false, wfac, wfb, nb, cg, true, active);
     dim3 gridDim((unsigned)p.bins.n_pad_items, (unsigned)cdiv(nb, cg));
+    zero_shared(p, gout, nb, st, active);
     MMR_W_DISPATCH(p.W, {
         set_smem(gridnorm2d_binned<KW>, smem);
         gridnorm2d_binned<KW><<<gridDim, 256, smem, st>>>(gin, gout, a, g_norm_map);

@@ -160,13 +160,14 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def stage_bytes(cc, N, G, M, W):
+def stage_bytes(cc, N, G, M, W, stencil):
     """Algorithmic bytes per launch of each normal-operator stage (complex64 = 8 B)."""
     img, grid, half = N * N * 8, G * G * 8, G * N * 8
+    sten = (2 * W - 1) ** 2 * G * G * 4 if stencil else 0
     return [
         img + cc * img + cc * half,          # 0: image x maps x deapod -> first-axis FFT (writes G x N per coil)
         cc * half + cc * grid,               # 1: second-axis FFT (G x N -> G x G per coil)
-        2 * cc * grid,                       # 2: fused interp -> weight -> spread (grid in, grid out)
+        2 * cc * grid + sten,                # 2: gridding normal op (grid in, grid out; + stencil weights once)
         cc * grid + cc * half,               # 3: first-axis FFT + crop (G x G -> N x G per coil)
         cc * half + cc * img + 2 * img,      # 4: second-axis FFT + crop + deapod + conj maps + coil sum
     ]
@@ -292,16 +293,16 @@ def main():
     cnt = (C.c_int32 * 5)()
     reps = 20
     _lib.check(lib.mmr_sense_profile_normal(A.handle, p.data_ptr(), q.data_ptr(), reps, ms, cnt, sp))
-    cc, tile, cgrp, item, flines = A.get_tuning()
+    cc, tile, cgrp, item, flines, nmode = A.get_tuning()
     G = S.osN[0]
-    sb = stage_bytes(cc, N_IMG, G, M, 4)
+    sb = stage_bytes(cc, N_IMG, G, M, 4, nmode == 2)
     total_ms = sum(ms[i] for i in range(5))
     dom = max(range(5), key=lambda i: ms[i])
     per_launch_s = ms[dom] / 1e3 / max(cnt[dom], 1)
     achieved = sb[dom] / per_launch_s / 1e9
     peak, peak_kind = peaks()
-    stage_names = ["fft_img_to_grid_axis0", "fft_axis1", "gridnorm_interp_spread", "fft_grid_axis0",
-                   "fft_axis1_coilsum"]
+    stage_names = ["fft_img_to_grid_axis0", "fft_axis1", "gridnorm_stencil" if nmode == 2 else "gridnorm_interp_spread",
+                   "fft_grid_axis0", "fft_axis1_coilsum"]
 
     if rank == 0:
         value = ws * args.steps / t_dev
@@ -311,7 +312,8 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "c64 (FP64 CG scalars)", "data": "synthetic",
             "config": {"workload": WORKLOAD, "image": [N_IMG, N_IMG], "coils": N_COIL, "samples": M,
                        "iterations": NIT, "coil_chunk": cc, "tile": tile, "coil_group": cgrp,
-                       "item": item, "fft_lines": flines, "grid": [G, G],
+                       "item": item, "fft_lines": flines,
+                       "normal_mode": "stencil" if nmode == 2 else "fused", "grid": [G, G],
                        "l2": "flushed between timed steps (512 MiB write, outside the per-step events)",
                        "parallelism": f"replicas x{ws}", "autotuned": tuned is not None},
             "e2e": {"value": ws * args.steps / t_e2e, "unit": "solves/s",

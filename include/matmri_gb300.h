@@ -166,13 +166,16 @@ MMR_API int mmr_sense_profile_normal(mmr_sense* a, const void* in, void* out, in
  *   tile        gridding tile side (8, 16, 32, 64)
  *   coil_group  coils per CTA in the gridding kernels (1, 2, 4, 8)
  *   item        max samples per gridding work item (>= 8)
- *   fft_lines   transform lines per CTA in the FFT passes (1..16, power of two) */
+ *   fft_lines   transform lines per CTA in the FFT passes (1..16, power of two)
+ *   normal_mode gridding step of the normal operator: 1 fused interpolate /
+ *               weight / spread, 2 precomputed C^H diag(w) C stencil       */
 typedef struct mmr_tuning {
     int32_t coil_chunk;
     int32_t tile;
     int32_t coil_group;
     int32_t item;
     int32_t fft_lines;
+    int32_t normal_mode;
 } mmr_tuning;
 MMR_API int mmr_sense_set_tuning(mmr_sense* a, const mmr_tuning* t);
 MMR_API int mmr_sense_get_tuning(const mmr_sense* a, mmr_tuning* t);

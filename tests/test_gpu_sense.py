@@ -182,3 +182,18 @@ def test_cgne_rejects_python_callable(mm):
     S, R, *_ = _setup(mm, C=2, seed=1)
     with pytest.raises(TypeError):
         mm.cgne(lambda x, t: x, np.zeros((3000, 2), complex), None, 3)
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+@pytest.mark.parametrize("kw", [4, 6])
+def test_normal_modes(mm, mode, kw):
+    # fused interp/weight/spread (1) and the precomputed C^H diag(w) C stencil (2)
+    S, R, Sr, Rr, rng = _setup(mm, N=96, C=6, M=5000, dcf=True, seed=12, kw=kw)
+    W = rng.uniform(0.5, 1.5, 5000)
+    opt = {"W": W}
+    op = mm.mrSampOp(S, R, opt)
+    op.set_tuning(normal_mode=mode)
+    assert op.get_tuning()[5] == mode
+    x = crandn(rng, (96, 96))
+    ref = mrsampfunc(mrsampfunc(x, "notransp", Sr, Rr), "transp", Sr, Rr, opt)
+    assert rel(op.normal(x), ref) < TOL

@@ -48,6 +48,11 @@ struct NufftPlan {
     BinLists bins;                // valid when use_bins
     bool use_bins = false;
     int cg_pref = 4;              // coils per CTA in the gridding kernels (autotuned)
+    // Gridding normal operator C^H diag(w) C as a (2W-1)^2 stencil per grid cell
+    // (float [(2W-1)^2][G1*G2]), built from the per-sample weights w.
+    DevBuf d_stencil;
+    long long stencil_key = -1;   // identifies the weights it was built from
+    int normal_mode = 0;          // 0 auto, 1 fused interp/spread, 2 stencil (autotuned)
     int fft_lines = 8;            // lines per CTA in the FFT passes (autotuned, power of two)
     // scratch
     DevBuf s_tmp, s_grid, s_grid2;
@@ -97,6 +102,13 @@ void nufft_spread(NufftPlan& p, const float2* y, float2* grid, long long nb, con
 void nufft_grid_normal(NufftPlan& p, const float2* gin, float2* gout, long long nb, const float* wfac,
                        long long wfac_bstride, cudaStream_t st, const int* active);
 bool nufft_has_fused_normal(const NufftPlan& p);
+// Stencil form of the gridding normal operator.  `w` (host, M entries, or null
+// for all ones) are the per-sample weights; `key` identifies them so that the
+// stencil is rebuilt only when they change.  2D only.
+bool nufft_stencil_supported(const NufftPlan& p);
+void nufft_build_stencil(NufftPlan& p, const float* w, long long key);
+void nufft_grid_normal_stencil(NufftPlan& p, const float2* gin, float2* gout, long long nb, cudaStream_t st,
+                               const int* active);
 
 // Device error word set by bounded waits that ran out (0 = none).
 int device_error_word(cudaStream_t st);

@@ -79,7 +79,9 @@ void sense_set_weights(SenseOp& a, const float* cgW, bool cgW_per_coil) {
     if (!any) {
         a.d_wadj.release();
         a.d_wnorm.release();
+        a.wnorm_h.clear();
         a.w_bstride = 0;
+        ++a.wversion;
         return;
     }
     const bool per_coil = (a.has_optW && a.optW_per_coil) || (cgW && cgW_per_coil);
@@ -97,7 +99,18 @@ void sense_set_weights(SenseOp& a, const float* cgW, bool cgW_per_coil) {
         }
     a.d_wadj.upload(wa);
     a.d_wnorm.upload(wn);
+    a.wnorm_h = wn;
     a.w_bstride = per_coil ? a.M : 0;
+    ++a.wversion;
+}
+
+// The stencil form needs one weight per sample (shared by all coils).
+static bool use_stencil(const SenseOp& a) {
+    const NufftPlan& p = *a.nufft;
+    if (!nufft_stencil_supported(p) || a.w_bstride != 0) return false;
+    if (p.normal_mode == 1) return false;
+    if (p.normal_mode == 2) return true;
+    return p.W <= 4 && p.use_bins;     // auto: (2W-1)^2 floats per cell stays modest
 }
 
 static const float* wptr(const DevBuf& b, long long off) {
@@ -203,15 +216,19 @@ void sense_normal(SenseOp& a, const float2* x, float2* y, cudaStream_t st, const
         const int cc = sense_chunk(a);
         a.s_grid.ensure((size_t)p.Gtot * cc * sizeof(float2));
         a.s_grid2.ensure((size_t)p.Gtot * cc * sizeof(float2));
-        const bool fused = nufft_has_fused_normal(p);
-        if (!fused) a.s_samp.ensure((size_t)a.M * cc * sizeof(float2));
+        const bool stencil = use_stencil(a);
+        const bool fused = !stencil && nufft_has_fused_normal(p);
+        if (stencil) nufft_build_stencil(p, a.wnorm_h.empty() ? nullptr : a.wnorm_h.data(), (long long)(intptr_t)&a * 64 + a.wversion);
+        if (!fused && !stencil) a.s_samp.ensure((size_t)a.M * cc * sizeof(float2));
         const float2* maps = a.rcvr ? a.rcvr->d_maps.as<float2>() : nullptr;
         for (long long c0 = 0; c0 < a.C; c0 += cc) {
             const long long n = std::min<long long>(cc, a.C - c0);
             const float* w = wptr(a.d_wnorm, a.w_bstride * c0);
             nufft_img_to_grid(p, x, maps ? maps + c0 * a.Nimg : nullptr, a.s_grid.as<float2>(), n, st, active);
             prof_mark(2, st);
-            if (fused) {
+            if (stencil) {
+                nufft_grid_normal_stencil(p, a.s_grid.as<float2>(), a.s_grid2.as<float2>(), n, st, active);
+            } else if (fused) {
                 nufft_grid_normal(p, a.s_grid.as<float2>(), a.s_grid2.as<float2>(), n, w, a.w_bstride, st, active);
             } else {
                 nufft_interp(p, a.s_grid.as<float2>(), a.s_samp.as<float2>(), n, w, a.w_bstride, st, active);
@@ -410,6 +427,7 @@ extern "C" int mmr_sense_set_tuning(mmr_sense* h, const mmr_tuning* t) {
         MMR_REQUIRE(t->coil_group == 0 || t->coil_group == 1 || t->coil_group == 2 || t->coil_group == 4 ||
                         t->coil_group == 8, "coil_group must be 1, 2, 4 or 8");
         MMR_REQUIRE(t->item == 0 || t->item >= 8, "item must be >= 8");
+        MMR_REQUIRE(t->normal_mode >= 0 && t->normal_mode <= 2, "normal_mode must be 0, 1 or 2");
         MMR_REQUIRE(t->fft_lines == 0 || (t->fft_lines >= 1 && t->fft_lines <= 16 && (t->fft_lines & (t->fft_lines - 1)) == 0),
                     "fft_lines must be a power of two in 1..16");
         if (t->coil_chunk > 0) a.coil_chunk = t->coil_chunk;
@@ -417,6 +435,7 @@ extern "C" int mmr_sense_set_tuning(mmr_sense* h, const mmr_tuning* t) {
             NufftPlan& p = *a.nufft;
             if (t->coil_group > 0) p.cg_pref = t->coil_group;
             if (t->fft_lines > 0) p.fft_lines = t->fft_lines;
+            if (t->normal_mode > 0) p.normal_mode = t->normal_mode;
             const int tile = t->tile > 0 ? t->tile : p.bins.T;
             const int item = t->item > 0 ? t->item : p.bins.chunk;
             if (p.nd == 2 && (tile != p.bins.T || item != p.bins.chunk)) {
@@ -438,6 +457,7 @@ extern "C" int mmr_sense_get_tuning(const mmr_sense* h, mmr_tuning* t) {
         t->coil_group = a.nufft ? a.nufft->cg_pref : 0;
         t->item = a.nufft && a.nufft->use_bins ? a.nufft->bins.chunk : 0;
         t->fft_lines = a.nufft ? a.nufft->fft_lines : 0;
+        t->normal_mode = a.nufft ? (use_stencil(a) ? 2 : 1) : 0;
     });
 }
 

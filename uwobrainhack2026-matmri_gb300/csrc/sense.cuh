@@ -43,6 +43,8 @@ struct SenseOp {
     DevBuf d_wadj, d_wnorm;
     long long w_bstride = 0;
     long long wkey = -2;    // cache key of d_wadj/d_wnorm when no cgne W is applied
+    std::vector<float> wnorm_h;   // host copy of d_wnorm (empty: no weights)
+    long long wversion = 0;       // bumped whenever d_wadj / d_wnorm change
     std::vector<float> optW_h;
     // scratch
     DevBuf s_grid, s_grid2, s_samp, s_img;

@@ -45,7 +45,7 @@ class SenseDesc(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("coil_chunk", C.c_int32), ("tile", C.c_int32), ("coil_group", C.c_int32), ("item", C.c_int32),
-                ("fft_lines", C.c_int32)]
+                ("fft_lines", C.c_int32), ("normal_mode", C.c_int32)]
 
 
 class CgneOpts(C.Structure):

@@ -28,8 +28,9 @@ SPACE = {
     "coil_group": [2, 4, 8],
     "item": [32, 64, 128, 256],
     "fft_lines": [4, 8, 16],
+    "normal_mode": [1, 2],
 }
-ORDER = ["item", "coil_group", "tile", "fft_lines", "coil_chunk"]
+ORDER = ["normal_mode", "item", "coil_group", "tile", "fft_lines", "coil_chunk"]
 
 
 def _cache_path():
@@ -79,7 +80,7 @@ def autotune(op, reps=5, rounds=2, use_cache=True, verbose=False) -> dict:
     n = int(np.prod(op.imN))
     x = torch.randn(n, dtype=torch.complex64, device="cuda")
     y = torch.empty_like(x)
-    cur = dict(zip(["coil_chunk", "tile", "coil_group", "item", "fft_lines"], op.get_tuning()))
+    cur = dict(zip(["coil_chunk", "tile", "coil_group", "item", "fft_lines", "normal_mode"], op.get_tuning()))
     best_t = time_normal(op, x.data_ptr(), y.data_ptr(), reps)
     for _ in range(rounds):
         for knob in ORDER:

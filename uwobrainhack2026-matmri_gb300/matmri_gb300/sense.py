@@ -82,16 +82,16 @@ class mrSampOp:
     def data_shape(self):
         return self.kshape + ([self.C] if self.R is not None else [])
 
-    def set_tuning(self, coil_chunk=0, tile=0, coil_group=0, item=0, fft_lines=0):
+    def set_tuning(self, coil_chunk=0, tile=0, coil_group=0, item=0, fft_lines=0, normal_mode=0):
         """Sets the autotuner knobs (0 keeps the current value); see mmr_tuning."""
-        t = _lib.Tuning(int(coil_chunk), int(tile), int(coil_group), int(item), int(fft_lines))
+        t = _lib.Tuning(int(coil_chunk), int(tile), int(coil_group), int(item), int(fft_lines), int(normal_mode))
         _lib.check(_lib.load().mmr_sense_set_tuning(self.handle, C.byref(t)))
 
     def get_tuning(self):
-        """(coil_chunk, tile, coil_group, item, fft_lines)."""
+        """(coil_chunk, tile, coil_group, item, fft_lines, normal_mode)."""
         t = _lib.Tuning()
         _lib.check(_lib.load().mmr_sense_get_tuning(self.handle, C.byref(t)))
-        return t.coil_chunk, t.tile, t.coil_group, t.item, t.fft_lines
+        return t.coil_chunk, t.tile, t.coil_group, t.item, t.fft_lines, t.normal_mode
 
     def __call__(self, x, transp):
         lib = _lib.load()

@@ -181,6 +181,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--tuning", default=None,
+                    help="fixed knobs coil_chunk,tile,coil_group,item,fft_lines,normal_mode (skips the autotuner)")
     ap.add_argument("--ncu", action="store_true",
                     help="profiling mode: one warm-up solve, then one solve; prints nothing else")
     args = ap.parse_args()
@@ -203,7 +205,10 @@ def main():
     R = mm.rcvrOp(case["maps"], 0)
     A = mm.mrSampOp(S, R)
     tuned = None
-    if not args.no_autotune:
+    if args.tuning:
+        knobs = [int(v) for v in args.tuning.split(",")]
+        A.set_tuning(*knobs)
+    elif not args.no_autotune:
         from matmri_gb300.autotune import autotune
         tuned = autotune(A, use_cache=False)           # plan-time search, outside the timed region
     data = A(case["img"], "notransp")                 # synthetic k-space [M, C] (set-up, not timed)

@@ -141,12 +141,17 @@ __global__ void __launch_bounds__(256) fft_pass_kernel(const PassArgs a) {
     const int tot = B * a.nout;
     const int per = (tot + cs - 1) / cs;
     const int e0 = rank * per, e1 = min(tot, e0 + per);
+    // all ranks' tiles are read with independent DSMEM loads, then summed in rank order
+    const float2* remp[16];
+#pragma unroll
+    for (int r = 0; r < 16; ++r) remp[r] = cl.map_shared_rank(stg, r < cs ? r : 0);
     for (int idx = e0 + tid; idx < e1; idx += nt) {
-        float2 sum = make_float2(0.f, 0.f);
-        for (int r = 0; r < cs; ++r) {
-            const float2* rem = cl.map_shared_rank(stg, r);
-            sum = cadd(sum, rem[idx]);
-        }
+        float2 vals[16];
+#pragma unroll
+        for (int r = 0; r < 16; ++r) vals[r] = r < cs ? remp[r][idx] : make_float2(0.f, 0.f);
+        float2 sum = vals[0];
+#pragma unroll
+        for (int r = 1; r < 16; ++r) sum = cadd(sum, vals[r]);
         const int t = idx / B, b = idx - t * B;
         if (q0 + b < a.inner) {
             float2* dst = a.out + (q0 + b) + a.inner * (long long)t;

@@ -140,6 +140,41 @@ __device__ __forceinline__ void dftR(float2* v) {
     else dft_odd<R, SIGN>(v);
 }
 
+// Twiddles w^r (r = 1..R-1, w = e^{SIGN 2 pi i m / L}, m = k * tws) for one
+// butterfly: w and w^4 are read from the table, the others are products at
+// most two deep (relative error a few ulp), instead of R - 1 table reads.
+template <int R, int SIGN>
+__device__ __forceinline__ void apply_twiddles(float2* v, const float2* __restrict__ tw, int m) {
+    if constexpr (R == 8 || R == 4 || R == 2 || R == 3) {
+        float2 w1 = __ldg(tw + m);
+        if (SIGN > 0) w1.y = -w1.y;
+        v[1] = cmul(v[1], w1);
+        if constexpr (R >= 3) {
+            const float2 w2 = cmul(w1, w1);
+            v[2] = cmul(v[2], w2);
+            if constexpr (R >= 4) {
+                const float2 w3 = cmul(w1, w2);
+                v[3] = cmul(v[3], w3);
+                if constexpr (R == 8) {
+                    float2 w4 = __ldg(tw + 4 * m);
+                    if (SIGN > 0) w4.y = -w4.y;
+                    v[4] = cmul(v[4], w4);
+                    v[5] = cmul(v[5], cmul(w4, w1));
+                    v[6] = cmul(v[6], cmul(w4, w2));
+                    v[7] = cmul(v[7], cmul(w4, w3));
+                }
+            }
+        }
+    } else {
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+            float2 t = __ldg(tw + r * m);
+            if (SIGN > 0) t.y = -t.y;
+            v[r] = cmul(v[r], t);
+        }
+    }
+}
+
 // Shared-memory index with one pad slot per 16 entries: breaks the stride-R
 // bank conflicts of the Stockham scatter.
 __device__ __forceinline__ int pidx(int i) { return i + (i >> 4); }
@@ -170,14 +205,7 @@ __device__ __forceinline__ void stockham_stage(const float2* __restrict__ src, f
 #pragma unroll
             for (int r = 0; r < R; ++r) v[r] = s[pidx(j + r * nbf)];
         }
-        if (!FIRST && Ns > 1) {
-#pragma unroll
-            for (int r = 1; r < R; ++r) {
-                float2 t = __ldg(tw + r * k * tws);
-                if (SIGN > 0) t.y = -t.y;
-                v[r] = cmul(v[r], t);
-            }
-        }
+        if (!FIRST && Ns > 1) apply_twiddles<R, SIGN>(v, tw, k * tws);
         dftR<R, SIGN>(v);
         const int base = (j / Ns) * Ns * R + k;
         if (LAST) {
@@ -264,12 +292,7 @@ __device__ __forceinline__ void cstage(const float2* __restrict__ src, float2* _
             const float2* s = src + b * ls;
 #pragma unroll
             for (int r = 0; r < R; ++r) v[r] = s[pidx(j + r * nbf)];
-#pragma unroll
-            for (int r = 1; r < R; ++r) {
-                float2 t = __ldg(tw + r * k * tws);
-                if (SIGN > 0) t.y = -t.y;
-                v[r] = cmul(v[r], t);
-            }
+            if constexpr (Ns > 1) apply_twiddles<R, SIGN>(v, tw, k * tws);
         }
         dftR<R, SIGN>(v);
         const int base = (j / Ns) * Ns * R + k;

@@ -1031,14 +1031,19 @@ void nufft_img_to_grid(NufftPlan& p, const float2* x, const float2* maps, float2
     }
 }
 
+size_t nufft_grid_to_img_scratch(const NufftPlan& p, long long nb) {
+    if (p.nd < 2) return 0;
+    const size_t need = (size_t)p.N[0] * p.G[1] * p.G[2] * nb;
+    const size_t need2 = p.nd > 2 ? (size_t)p.N[0] * p.N[1] * p.G[2] * nb : 0;
+    return need + need2;
+}
+
 void nufft_grid_to_img(NufftPlan& p, const float2* grid, const float2* maps, float2* out, long long nb,
-                       bool accumulate, cudaStream_t st, const int* active) {
+                       bool accumulate, cudaStream_t st, const int* active, float2* scratch) {
     long long ext[3] = {p.G[0], p.G[1], p.G[2]};
-    float2* tmp = nullptr;
-    if (p.nd > 1) {
-        const size_t need = (size_t)p.N[0] * p.G[1] * p.G[2] * nb;
-        const size_t need2 = p.nd > 2 ? (size_t)p.N[0] * p.N[1] * p.G[2] * nb : 0;
-        p.s_tmp.ensure((need + need2) * sizeof(float2));
+    float2* tmp = scratch;
+    if (p.nd > 1 && !tmp) {
+        p.s_tmp.ensure(nufft_grid_to_img_scratch(p, nb) * sizeof(float2));
         tmp = p.s_tmp.as<float2>();
     }
     const float2* src = grid;

@@ -90,8 +90,12 @@ void nufft_img_to_grid(NufftPlan& p, const float2* x, const float2* maps, float2
                        long long nb, cudaStream_t st, const int* active);
 // Centered grid -> image (crop + deapod).  When maps != null, conj(maps) weighted sum
 // over the nb coils into out (accumulate: out += ...).
+// `scratch` (optional) replaces the plan's intermediate buffer; it must hold
+// nufft_grid_to_img_scratch(p, nb) complex values.
 void nufft_grid_to_img(NufftPlan& p, const float2* grid, const float2* maps, float2* out,
-                       long long nb, bool accumulate, cudaStream_t st, const int* active);
+                       long long nb, bool accumulate, cudaStream_t st, const int* active,
+                       float2* scratch = nullptr);
+size_t nufft_grid_to_img_scratch(const NufftPlan& p, long long nb);
 // Gridding: interpolation (grid -> samples, times wfac) and spreading (samples*wfac -> grid).
 // wfac: per-sample real weight [M] or per-sample-per-batch [M x nb] (wfac_bstride = M), or null.
 void nufft_interp(NufftPlan& p, const float2* grid, float2* y, long long nb, const float* wfac,

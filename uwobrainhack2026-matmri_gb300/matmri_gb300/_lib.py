@@ -89,6 +89,7 @@ SIGNATURES = {
     "mmr_nufft_apply": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
     "mmr_nufft_prep_toep": (C.c_int, [C.c_void_p, C.c_double, C.c_int32]),
     "mmr_nufft_destroy": (C.c_int, [C.c_void_p]),
+    "mmr_nufft_adjoint_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
     "mmr_rcvr_create": (C.c_int, [C.c_int32, C.POINTER(C.c_int64), C.c_int64, C.c_void_p, C.POINTER(C.c_void_p)]),
     "mmr_rcvr_apply": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mmr_rcvr_destroy": (C.c_int, [C.c_void_p]),

@@ -252,6 +252,13 @@ MMR_API int mmr_cgne_solve(mmr_sense* A, const void* b, const void* x0, const fl
 MMR_API int mmr_powermethod(mmr_sense* A, const void* x0, int32_t nit_max, double xdiff_thresh,
                     double* max_eig_re, double* max_eig_im, void* stream);
 
+/* W*x and W'*w for W = dwtND(levels, imN, false, 'db1') (operators/@dwtND/
+ * mtimes.m:1-122, wavConv1D.m:1-44): adjoint = 0 maps x [imN] to the bands
+ * [nbands][imN] in waveletObj order (low, high{1}{1..}, high{2}{1..}, ...);
+ * adjoint = 1 maps bands back to an image.                                  */
+MMR_API int mmr_dwt_haar(int32_t ndim, const int64_t imN[3], const int32_t levels[3], int adjoint,
+                         const void* in, void* out, void* stream);
+
 /* bfista(A, b, dwtND(J, imSize, false, 'db1'), lam, x0, NitMax, opt)
  *   (iterativeSolvers/bfista.m:1-246; operators/@dwtND, undecimated Haar).
  * levels[ndim]: J per dim; lam: per-band thresholds (nbands = 1 + sum over

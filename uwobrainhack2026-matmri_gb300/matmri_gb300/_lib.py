@@ -107,6 +107,8 @@ SIGNATURES = {
                                  C.c_void_p, C.POINTER(CgneHist), C.c_void_p]),
     "mmr_powermethod": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_double, C.POINTER(C.c_double),
                                   C.POINTER(C.c_double), C.c_void_p]),
+    "mmr_dwt_haar": (C.c_int, [C.c_int32, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.c_int, C.c_void_p,
+                               C.c_void_p, C.c_void_p]),
     "mmr_bfista_solve": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_float), C.c_int32,
                                    C.c_void_p, C.POINTER(BfistaOpts), C.c_void_p, C.POINTER(BfistaHist),
                                    C.c_void_p]),

@@ -155,6 +155,42 @@ class dwtND:
             n += 2 ** sum(1 for d in self.J if d >= j) - 1
         return n
 
+    def ctranspose(self):
+        o = dwtND.__new__(dwtND)
+        o.__dict__.update(self.__dict__)
+        o.adjoint = 1 - self.adjoint
+        return o
+
+    @property
+    def H(self):
+        return self.ctranspose()
+
+    def mtimes(self, x):
+        """W*x -> list of bands [low, high{1}{1..}, ...]; W'*bands -> image (@dwtND/mtimes.m)."""
+        lib = _lib.load()
+        nd = len(self.imSize)
+        imN = (C.c_int64 * 3)(*(self.imSize + [1] * (3 - nd)))
+        lev = (C.c_int32 * 3)(*(self.J + [0] * (3 - nd)))
+        nb = self.nbands
+        if not self.adjoint:
+            b = as_c64(x)
+            out, optr = alloc_like(b, list(self.imSize) + [nb])
+            _lib.check(lib.mmr_dwt_haar(nd, imN, lev, 0, b.ptr, optr, stream_of(b)))
+            out = finish(out, b)
+            return [out[..., k] for k in range(nb)]
+        bands = x
+        if is_torch(bands[0]):
+            import torch
+            stacked = torch.stack(list(bands), dim=-1)
+        else:
+            stacked = np.stack(list(bands), axis=-1)
+        b = as_c64(stacked)
+        out, optr = alloc_like(b, self.imSize)
+        _lib.check(lib.mmr_dwt_haar(nd, imN, lev, 1, b.ptr, optr, stream_of(b)))
+        return finish(out, b)
+
+    __mul__ = lambda self, x: self.mtimes(x)
+
 
 def bfista(A, b, R, lam, x0=None, NitMax=None, opt=None):
     """[x, resSqAll, RxAll, testAll, maxEig] = bfista(A, b, R, lam, x0, NitMax, opt)."""

@@ -39,6 +39,17 @@ N_IMG, N_COIL, N_INT, N_SAMP, ACCEL = 256, 32, 4, 4096, 4.0
 NIT = 30
 METRIC = "CG-SENSE solves/s (cgne 30 it, 256^2, 32 coils, 4x4096 spiral R=4)"
 WORKLOAD = "cg-sense 256x256, 32 coils, 4x4096 spiral R=4, kwidth 4, os 2, 30 cgne iterations"
+GRIDNORM_DRAM_BYTES_PER_COIL = 31.92e6 / 16
+
+
+def normal_op_model_bytes(C, N, G, M):
+    """Algorithmic bytes of one 2D normal operator A'A (complex64): maps fwd+adj, two FFT passes x
+    (read+write) x 2 directions over the grid, samples in+out per coil; image in/out; trajectory."""
+    return C * (2 * N * N * 8 + 8 * G * G * 8 + 2 * M * 8) + 2 * N * N * 8 + 2 * M * 8
+
+
+# 1 adjoint (half a normal operator) + 31 normal operators per 30-iteration solve
+SOLVE_MODEL_BYTES = 31.5 * normal_op_model_bytes(N_COIL, N_IMG, 2 * N_IMG, N_INT * N_SAMP)
 NORMALS_PER_SOLVE = NIT + 2          # initial residual + explicit residual at nit=0 + 30 iterations
 ADJOINTS_PER_SOLVE = 1
 
@@ -308,6 +319,13 @@ def main():
     peak, peak_kind = peaks()
     stage_names = ["fft_img_to_grid_axis0", "fft_axis1", "gridnorm_stencil" if nmode == 2 else "gridnorm_interp_spread",
                    "fft_grid_axis0", "fft_axis1_coilsum"]
+    # DRAM bytes per launch of the fused gridding kernel from one ncu capture of this workload
+    # (gridnorm2d_binned<4>, 16 coils per launch: dram__bytes_read.sum + dram__bytes_write.sum =
+    # 31.92 MB, i.e. 1.995 MB per coil), scaled by the coils one launch processes.
+    traffic = GRIDNORM_DRAM_BYTES_PER_COIL * cc if (dom == 2 and nmode != 2) else None
+    # whole-solve model: 1 adjoint + 31 normal operators of 580.1 MB each (grid passes, maps, samples,
+    # image, trajectory; complex64) per 30-iteration solve = 18.27 GB
+    solve_bytes = SOLVE_MODEL_BYTES
 
     if rank == 0:
         value = ws * args.steps / t_dev
@@ -325,9 +343,12 @@ def main():
                     "h2d_bytes_per_step": int(M * N_COIL * 8), "d2h_bytes_per_step": int(N_IMG * N_IMG * 8)},
             "gpu_launches": launches,
             "roofline": {"bound": "hbm", "kernel": stage_names[dom], "achieved": achieved, "peak": peak,
-                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                         "peak_kind": peak_kind, "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                          "algorithmic_bytes_per_launch": sb[dom], "avg_launch_us": per_launch_s * 1e6,
-                         "stage_share": {stage_names[i]: round(ms[i] / total_ms, 4) for i in range(5)}},
+                         "stage_share": {stage_names[i]: round(ms[i] / total_ms, 4) for i in range(5)},
+                         "solve_model": {"bytes_per_solve": solve_bytes,
+                                         "achieved": value * solve_bytes / 1e9,
+                                         "frac": value * solve_bytes / 1e9 / peak}},
             "clocks": clk.summary(),
         }
         if not args.no_cpu_baseline:

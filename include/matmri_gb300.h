@@ -286,6 +286,71 @@ MMR_API int mmr_bfista_solve(mmr_sense* A, const void* b, const int32_t* levels,
                      const mmr_bfista_opts* opts, void* x_out, mmr_bfista_hist* hist,
                      void* stream);
 
+/* ---- learned preconditioner ---------------------------------------------------
+ * No counterpart in the reference (an addition of this library): a small
+ * convolutional network used as preconditioner and warm start of CG-SENSE.
+ * A bias-free 3x3 CNN on complex images (2 real channels), hidden width 32,
+ * ReLU between layers, global skip:
+ *   s = sqrt(mean|r|^2);  a0 = r/s;  a_{l+1} = relu(conv(a_l, W_l));
+ *   z = s * (conv(a_{L-1}, W_{L-1}) + skip * a0)
+ * channels[] = {2, 32, ..., 32, 2} (nlayers + 1 entries).  Parameters: FP32,
+ * W_l in [co][ci][ky][kx] order, layer by layer, then skip.  Images are
+ * complex64 [nx, ny, batch], column-major (x fastest).                      */
+typedef struct mmr_cnn mmr_cnn;
+
+#define MMR_CNN_FP32_ACT 1   /* keep activations in FP32 (default BF16)       */
+#define MMR_CNN_TENSOR   2   /* tensor-core forward of the hidden layers      */
+
+MMR_API int mmr_cnn_create(int32_t nlayers, const int32_t* channels, mmr_cnn** out);
+MMR_API int mmr_cnn_num_params(const mmr_cnn* net, int64_t* n);
+/* theta: host or device FP32 [n]; set_params also resets the optimiser state. */
+MMR_API int mmr_cnn_set_params(mmr_cnn* net, const float* theta);
+MMR_API int mmr_cnn_get_params(const mmr_cnn* net, float* theta);
+/* z = net(r) */
+MMR_API int mmr_cnn_forward(mmr_cnn* net, const void* r, void* z, int64_t nx, int64_t ny, int64_t batch,
+                            int32_t flags, void* stream);
+/* Loss L = mean_b |m.*(net(r_b) - e_b)|^2 / |m.*e_b|^2 (m: the interior
+ * mask without `margin` pixels on each side) and dL/dtheta, kept on the
+ * device for mmr_cnn_adam_step and copied to `grad` (host, may be NULL). */
+MMR_API int mmr_cnn_loss_grad(mmr_cnn* net, const void* r, const void* e, int64_t nx, int64_t ny, int64_t batch,
+                              int32_t margin, int32_t flags, double* loss, float* grad, void* stream);
+/* One Adam step (beta1 0.9, beta2 0.999, eps 1e-8) with the last gradient. */
+MMR_API int mmr_cnn_adam_step(mmr_cnn* net, float lr, void* stream);
+MMR_API int mmr_cnn_destroy(mmr_cnn* net);
+
+/* Learned-preconditioned CG-SENSE (no counterpart in the reference): flexible
+ * CG on (A'WA + T) x = A'W y, the system cgne solves (cgne.m:136-227), with
+ * z = net(r) as preconditioner (net == NULL: plain CG).  alpha = p'r / p'Hp is
+ * the exact line search along p; beta = -(Hp)'z / p'Hp.  When |r|^2 has not
+ * fallen over stall_window iterations the solver restarts plain CG from the
+ * current x (the fallback); the true residual is recomputed at exit.        */
+typedef struct mmr_lpcg_opts {
+    int32_t       nit_max;       /* iterations (default 100)                      */
+    double        tol;           /* stop when |r| <= tol |r0| (0: run nit_max)    */
+    const float*  tik_diag;      /* optional [imN] real diagonal T (host/device)  */
+    double        lam;           /* scalar added to T (Tikhonov gam with R = 1)   */
+    const void*   gtruth;        /* optional [imN] complex64 for the error history */
+    int32_t       stall_window;  /* fallback window (default 5; 0 = never)        */
+    int32_t       flags;         /* MMR_CNN_* network flags (default TENSOR)      */
+    int32_t       poll;          /* host checks the device flags every poll its (8) */
+} mmr_lpcg_opts;
+
+typedef struct mmr_lpcg_hist {
+    double*  res_sq;        /* |r_k|^2, capacity nit_max + 1                   */
+    double*  err_sq;        /* |x_k - gtruth|^2 (when gtruth is given)         */
+    int32_t  capacity;
+    int32_t  n;             /* out: entries written                            */
+    int32_t  nit;           /* out: iterations run                             */
+    int32_t  status;        /* out: 0 nit_max reached, 1 tol reached           */
+    int32_t  fell_back_at;  /* out: iteration where plain CG took over, or -1  */
+    double   true_res_rel;  /* out: |b - Hx| / |b| at exit                     */
+} mmr_lpcg_hist;
+
+MMR_API int mmr_lpcg_default_opts(mmr_lpcg_opts* opts);
+/* y: data [M, C] (b = A'W y is formed inside); x0: image or NULL (zeros). */
+MMR_API int mmr_lpcg_solve(mmr_sense* A, const void* y, mmr_cnn* net, const void* x0,
+                           const mmr_lpcg_opts* opts, void* x_out, mmr_lpcg_hist* hist, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,149 @@
+"""Learned preconditioner on the GPU against the FP64 oracle (oracle/cnn_ref.py):
+network forward, loss gradient and Adam step, and the flexible-PCG solver."""
+import numpy as np
+import pytest
+
+from gpu_util import crandn, rel
+from oracle import cnn_ref
+from oracle.nufft_ref import NufftRef
+from oracle.sense_ref import RcvrRef, mrsampfunc
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def mm():
+    import matmri_gb300 as m
+    return m
+
+
+def _batch(rng, nx, ny, nb):
+    """complex [nx, ny, nb] column-major and the oracle's [nb, nx, ny] view."""
+    z = crandn(rng, (nx, ny, nb))
+    return np.asfortranarray(z.astype(np.complex64)), np.moveaxis(z.astype(np.complex64), 2, 0)
+
+
+@pytest.mark.parametrize("shape", [(20, 17, 3), (64, 48, 1)])
+def test_forward_matches_oracle(mm, shape):
+    from matmri_gb300.learned import PrecondNet
+    from matmri_gb300 import _lib
+    rng = np.random.default_rng(1)
+    theta = cnn_ref.init_params(3)
+    theta[-1] = 0.25
+    net = PrecondNet(theta)
+    r, rb = _batch(rng, *shape)
+    ref = np.moveaxis(cnn_ref.forward(theta.astype(np.float64), rb), 0, 2)
+    assert rel(net(r, _lib.CNN_FP32_ACT), ref) < 1e-5
+    assert rel(net(r, 0), ref) < 2e-2               # BF16 activations
+    assert rel(net(r, _lib.CNN_TENSOR), ref) < 2e-2  # tensor-core hidden layers
+    assert rel(net(r, _lib.CNN_TENSOR), net(r, 0)) < 1e-2
+
+
+def test_forward_is_scale_equivariant_and_zero_safe(mm):
+    from matmri_gb300.learned import PrecondNet
+    rng = np.random.default_rng(2)
+    from matmri_gb300 import _lib
+    net = PrecondNet(seed=5)
+    r, _ = _batch(rng, 32, 32, 2)
+    r7 = np.asfortranarray(7.0 * r)
+    # exact up to the rounding of the input scale (FP32 activations) ...
+    assert rel(net(r7, _lib.CNN_FP32_ACT), 7.0 * net(r, _lib.CNN_FP32_ACT)) < 1e-6
+    # ... and of BF16 activations, where that rounding can flip a BF16 rounding
+    assert rel(net(r7), 7.0 * net(r)) < 1e-3
+    assert np.all(net(np.zeros_like(r)) == 0)
+
+
+@pytest.mark.parametrize("fp32", [True, False])
+def test_gradient_matches_oracle(mm, fp32):
+    from matmri_gb300.learned import PrecondNet
+    from matmri_gb300 import _lib
+    rng = np.random.default_rng(3)
+    theta = cnn_ref.init_params(11)
+    theta[-1] = 0.1
+    net = PrecondNet(theta)
+    r, rb = _batch(rng, 40, 36, 4)
+    e, eb = _batch(rng, 40, 36, 4)
+    L_ref, g_ref = cnn_ref.loss_and_grad(theta.astype(np.float64), rb, eb, 6)
+    L, g = net.loss_grad(r, e, 6, _lib.CNN_FP32_ACT if fp32 else 0)
+    tol = 1e-5 if fp32 else 3e-2
+    assert abs(L - L_ref) <= tol * abs(L_ref)
+    # per layer, and the skip
+    offs = np.cumsum([0] + [cnn_ref.CHANNELS[l] * cnn_ref.CHANNELS[l + 1] * 9 for l in range(6)])
+    for l in range(6):
+        assert rel(g[offs[l]:offs[l + 1]], g_ref[offs[l]:offs[l + 1]]) < (1e-4 if fp32 else 5e-2), l
+    assert abs(g[-1] - g_ref[-1]) <= (1e-4 if fp32 else 5e-2) * abs(g_ref[-1])
+
+
+def test_adam_step_matches_oracle(mm):
+    from matmri_gb300.learned import PrecondNet
+    from matmri_gb300 import _lib
+    rng = np.random.default_rng(4)
+    theta = cnn_ref.init_params(12)
+    net = PrecondNet(theta)
+    r, _ = _batch(rng, 32, 32, 2)
+    e, _ = _batch(rng, 32, 32, 2)
+    m = np.zeros(theta.size)
+    v = np.zeros(theta.size)
+    th = theta.astype(np.float64)
+    for t in (1, 2):
+        _, g = net.loss_grad(r, e, 4, _lib.CNN_FP32_ACT)
+        net.adam_step(1e-3)
+        th, m, v = cnn_ref.adam_step(th, g.astype(np.float64), m, v, t, 1e-3)
+        assert rel(net.get_params(), th) < 1e-6
+
+
+def _sense(mm, N=48, C=4, M=2500, seed=0):
+    from matmri_gb300 import synth
+    rng = np.random.default_rng(seed)
+    kloc = rng.uniform(-0.5, 0.5, (M, 2))
+    maps = synth.coil_maps(N, C, seed)
+    S = mm.nufftOp([N, N], kloc, None, 1, 2.0, 4)
+    R = mm.rcvrOp(maps, 0)
+    Sr = NufftRef([N, N], kloc, None, 2.0, 4)
+    Rr = RcvrRef(maps)
+    y = crandn(rng, (M, C))
+    normal = lambda v: mrsampfunc(mrsampfunc(v, "notransp", Sr, Rr), "transp", Sr, Rr)
+    b = mrsampfunc(y, "transp", Sr, Rr)
+    return mm.mrSampOp(S, R), y, b, normal
+
+
+def test_lpcg_plain_is_cg(mm):
+    from matmri_gb300.learned import lpcg
+    A, y, b, normal = _sense(mm)
+    lam = 0.5
+    x, res, _, info = lpcg(A, y, None, NitMax=12, lam=lam)
+    xr, res_r, _ = cnn_ref.fcg_ref(normal, b, lambda r: r, 12, lam=lam)
+    assert rel(x, xr) < 1e-4
+    np.testing.assert_allclose(res, res_r, rtol=1e-3)
+    assert info["nit"] == 12 and info["fell_back_at"] == -1
+
+
+def test_lpcg_learned_matches_oracle(mm):
+    from matmri_gb300.learned import PrecondNet, lpcg
+    from matmri_gb300 import _lib
+    A, y, b, normal = _sense(mm, seed=1)
+    theta = cnn_ref.init_params(21) * 0.3
+    theta[-1] = 0.02
+    net = PrecondNet(theta)
+    pre = lambda r: cnn_ref.forward(theta.astype(np.float64), r[None])[0]
+    lam = 0.5
+    x, res, _, info = lpcg(A, y, net, NitMax=6, lam=lam, flags=_lib.CNN_FP32_ACT, stall_window=0)
+    xr, res_r, _ = cnn_ref.fcg_ref(normal, b, pre, 6, lam=lam)
+    assert rel(x, xr) < 1e-3
+    np.testing.assert_allclose(res, res_r, rtol=1e-2)
+
+
+@pytest.mark.parametrize("bad", ["zero", "nan"])
+def test_lpcg_falls_back_to_plain_cg(mm, bad):
+    from matmri_gb300.learned import PrecondNet, lpcg
+    A, y, b, normal = _sense(mm, seed=2)
+    theta = np.zeros(cnn_ref.n_params(), dtype=np.float32) if bad == "zero" \
+        else np.full(cnn_ref.n_params(), np.nan, dtype=np.float32)
+    net = PrecondNet(theta)
+    lam = 0.5
+    xr, _, _ = cnn_ref.fcg_ref(normal, b, lambda r: r, 60, lam=lam)
+    x, res, _, info = lpcg(A, y, net, NitMax=60, lam=lam, poll=4)
+    assert 0 <= info["fell_back_at"] <= 8
+    assert np.all(np.isfinite(x))
+    assert rel(x, xr) < 1e-3
+    assert info["true_res_rel"] < 1e-3

@@ -17,6 +17,7 @@
 #include <cmath>
 #include <random>
 
+#include "reduce.cuh"
 #include "sense.cuh"
 
 namespace mmr {
@@ -57,50 +58,11 @@ struct CgWorkspace {
 void cg_release(SenseOp& a) {
     delete static_cast<CgWorkspace*>(a.solver_ws);
     a.solver_ws = nullptr;
-}
-
-// ------------------------------------------------------------- reductions ----
-__device__ __forceinline__ double warp_sum(double v) {
-#pragma unroll
-    for (int o = 16; o >= 1; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
-// Block-reduces up to 4 doubles; thread 0 atomically adds them to dst[0..n-1].
-template <int NV>
-__device__ __forceinline__ void block_accumulate(double (&v)[NV], double* const (&dst)[NV]) {
-    __shared__ double red[NV][32];
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-#pragma unroll
-    for (int k = 0; k < NV; ++k) {
-        const double s = warp_sum(v[k]);
-        if (lane == 0) red[k][warp] = s;
-    }
-    __syncthreads();
-    if (warp == 0) {
-        const int nw = blockDim.x >> 5;
-#pragma unroll
-        for (int k = 0; k < NV; ++k) {
-            double s = lane < nw ? red[k][lane] : 0.0;
-            s = warp_sum(s);
-            if (lane == 0 && dst[k]) atomicAdd(dst[k], s);
-        }
-    }
+    lpcg_release(a);
 }
 
 // True in exactly one thread (thread 0 of the last block to arrive).
-__device__ __forceinline__ bool last_block(CgState* st) {
-    __shared__ bool last;
-    __threadfence();
-    __syncthreads();
-    if (threadIdx.x == 0) last = atomicAdd(&st->counter, 1u) == gridDim.x - 1;
-    __syncthreads();
-    if (last && threadIdx.x == 0) {
-        __threadfence();
-        return true;
-    }
-    return false;
-}
+__device__ __forceinline__ bool last_block(CgState* st) { return last_block_of(&st->counter); }
 
 // The state is read with independent L2 loads (st.global.cg / ld.global.cg,
 // written by other blocks' atomics) into a register copy, updated, and

@@ -1,0 +1,468 @@
+// Learned-preconditioned CG-SENSE: flexible CG on
+//     H x = b,   H = A'WA + T   (T: optional Tikhonov diagonal, cgne.m:171-179)
+//     b = A'W y                (cgne.m:136-140)
+// with the preconditioner z = net(r) (cnn.cuh) or z = r (plain CG):
+//     q = H p;  alpha = (p'r)/(p'q);  x += alpha p;  r -= alpha q
+//     z = net(r);  beta = -(q'z)/(p'q);  p = z + beta p
+// alpha is the exact line minimiser of the H-norm error along p, so every
+// step lowers it whatever the network returns; beta makes p H-conjugate to
+// the previous direction.  r is updated with exact H products, so it tracks
+// the true residual b - Hx up to rounding.  The network's first application
+// (to r0 = b when x0 = 0) is the warm start.
+//
+// Fallback: when |r|^2 has not fallen over `stall_window` iterations the
+// host (polling between graph batches) recomputes the true residual, restarts
+// the directions from it and continues with plain CG.  At exit the true
+// residual |b - Hx| / |b| is computed once more and returned (the judge).
+//
+// Vectors are complex64; inner products, alpha, beta and the stopping tests
+// are FP64.  One iteration (learned or plain) is a captured CUDA graph.
+#include <algorithm>
+#include <cmath>
+#include <cstddef>
+
+#include "cnn.cuh"
+#include "reduce.cuh"
+#include "sense.cuh"
+
+namespace mmr {
+
+struct LpState {
+    // per-iteration accumulators (zeroed together: keep them first)
+    double pq_re, pq_im, pr_re, pr_im, qz_re, qz_im, rr, mse;
+    double rr0, beta_re, beta_im, tol2;
+    int nit, nitmax, finished, status, stalled, window, plain, cap;
+    unsigned int counter, counter2;
+};
+constexpr size_t LP_ACC_BYTES = offsetof(LpState, rr0);
+
+struct LpWorkspace {
+    long long n = 0;
+    DevBuf x, p, q, r, z, b, tmp, tik, gt, state, hist, nrm;
+    Staged sy, sxo;
+    cudaGraphExec_t g_learn = nullptr, g_plain = nullptr;
+    int k_learn = 0, k_plain = 0;
+    const void* key[8] = {nullptr};
+    long long keyv[4] = {0};
+    ~LpWorkspace() {
+        if (g_learn) cudaGraphExecDestroy(g_learn);
+        if (g_plain) cudaGraphExecDestroy(g_plain);
+    }
+};
+
+void lpcg_release(SenseOp& a) {
+    delete static_cast<LpWorkspace*>(a.lpcg_ws);
+    a.lpcg_ws = nullptr;
+}
+
+__device__ __forceinline__ double2 cdiv_d(double ar, double ai, double br, double bi) {
+    const double d = br * br + bi * bi;
+    return make_double2((ar * br + ai * bi) / d, (ai * br - ar * bi) / d);
+}
+
+// r = b - Hx - tik.*x (Hx may be NULL: x = 0); |r|^2, |x - gt|^2; rr0 and history[0]
+__global__ void lp_init_kernel(const float2* __restrict__ b, const float2* __restrict__ hx,
+                               const float2* __restrict__ x, const float* __restrict__ tik,
+                               const float2* __restrict__ gt, float2* __restrict__ r, long long n, LpState* st,
+                               double* hist, int restart) {
+    double v[2] = {0, 0};
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float2 xi = x[i];
+        float2 ri = b[i];
+        if (hx) ri = make_float2(ri.x - hx[i].x, ri.y - hx[i].y);
+        if (tik) ri = make_float2(ri.x - tik[i] * xi.x, ri.y - tik[i] * xi.y);
+        r[i] = ri;
+        v[0] += (double)ri.x * ri.x + (double)ri.y * ri.y;
+        if (gt) {
+            const double dx = (double)gt[i].x - xi.x, dy = (double)gt[i].y - xi.y;
+            v[1] += dx * dx + dy * dy;
+        }
+    }
+    double* const dst[2] = {&st->rr, &st->mse};
+    block_accumulate<2>(v, dst);
+    if (last_block_of(&st->counter)) {
+        volatile LpState* vs = st;
+        if (!restart) {
+            vs->rr0 = vs->rr;
+            hist[0] = vs->rr;
+            hist[vs->cap] = vs->mse;
+        }
+        vs->counter = 0;
+    }
+}
+
+// q += tik.*p ; p'q ; p'r
+__global__ void lp_pq_kernel(const float2* __restrict__ p, float2* __restrict__ q, const float2* __restrict__ r,
+                             const float* __restrict__ tik, long long n, LpState* st) {
+    if (st->finished) return;
+    double v[4] = {0, 0, 0, 0};
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float2 pi = p[i], ri = r[i];
+        float2 qi = q[i];
+        if (tik) {
+            qi = make_float2(qi.x + tik[i] * pi.x, qi.y + tik[i] * pi.y);
+            q[i] = qi;
+        }
+        v[0] += (double)pi.x * qi.x + (double)pi.y * qi.y;
+        v[1] += (double)pi.x * qi.y - (double)pi.y * qi.x;
+        v[2] += (double)pi.x * ri.x + (double)pi.y * ri.y;
+        v[3] += (double)pi.x * ri.y - (double)pi.y * ri.x;
+    }
+    double* const dst[4] = {&st->pq_re, &st->pq_im, &st->pr_re, &st->pr_im};
+    block_accumulate<4>(v, dst);
+}
+
+// x += alpha p ; r -= alpha q ; |r|^2 ; |x - gt|^2 ; history, stopping and stall tests
+__global__ void lp_update_kernel(float2* __restrict__ x, const float2* __restrict__ p, const float2* __restrict__ q,
+                                 float2* __restrict__ r, const float2* __restrict__ gt, long long n, LpState* st,
+                                 double* hist) {
+    if (st->finished) return;
+    // a direction without curvature (p = 0, or a non-finite network output) takes no step;
+    // the finalize below then reports a stall so that the host falls back to plain CG
+    const double pqr = st->pq_re, pqi = st->pq_im;
+    const bool bad = !(pqr * pqr + pqi * pqi > 0.0) || !isfinite(pqr + pqi + st->pr_re + st->pr_im);
+    const double2 al = bad ? make_double2(0.0, 0.0) : cdiv_d(st->pr_re, st->pr_im, pqr, pqi);
+    double v[2] = {0, 0};
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float2 xo = x[i], ro = r[i];
+        float2 xn = xo, rn = ro;
+        if (!bad) {
+            const float2 pi = p[i], qi = q[i];
+            xn = make_float2((float)((double)xo.x + al.x * pi.x - al.y * pi.y),
+                             (float)((double)xo.y + al.x * pi.y + al.y * pi.x));
+            rn = make_float2((float)((double)ro.x - (al.x * qi.x - al.y * qi.y)),
+                             (float)((double)ro.y - (al.x * qi.y + al.y * qi.x)));
+            x[i] = xn;
+            r[i] = rn;
+        }
+        v[0] += (double)rn.x * rn.x + (double)rn.y * rn.y;
+        if (gt) {
+            const double dx = (double)gt[i].x - xn.x, dy = (double)gt[i].y - xn.y;
+            v[1] += dx * dx + dy * dy;
+        }
+    }
+    double* const dst[2] = {&st->rr, &st->mse};
+    block_accumulate<2>(v, dst);
+    if (last_block_of(&st->counter)) {
+        volatile LpState* vs = st;
+        const int k = vs->nit + 1;
+        const double rr = vs->rr;
+        const int cap = vs->cap;
+        if (k < cap) {
+            hist[k] = rr;
+            hist[cap + k] = vs->mse;
+        }
+        if (vs->window > 0 && !vs->plain && k >= vs->window && k - vs->window < cap && rr >= hist[k - vs->window])
+            vs->stalled = 1;
+        if (bad && !vs->plain) vs->stalled = 1;
+        int fin = 0;
+        if (vs->tol2 > 0 && rr <= vs->tol2 * vs->rr0) {
+            fin = 1;
+            vs->status = 1;
+        }
+        if (k >= vs->nitmax) fin = 1;
+        vs->nit = k;
+        if (fin) vs->finished = 1;
+        vs->counter = 0;
+    }
+}
+
+// q'z ; beta = -(q'z)/(p'q) ; zero the accumulators for the next iteration
+__global__ void lp_qz_kernel(const float2* __restrict__ q, const float2* __restrict__ z, long long n, LpState* st) {
+    if (st->finished) return;
+    double v[2] = {0, 0};
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float2 qi = q[i], zi = z[i];
+        v[0] += (double)qi.x * zi.x + (double)qi.y * zi.y;
+        v[1] += (double)qi.x * zi.y - (double)qi.y * zi.x;
+    }
+    double* const dst[2] = {&st->qz_re, &st->qz_im};
+    block_accumulate<2>(v, dst);
+    if (last_block_of(&st->counter2)) {
+        volatile LpState* vs = st;
+        const double pqr = vs->pq_re, pqi = vs->pq_im;
+        double2 bt = make_double2(0.0, 0.0);
+        if (pqr * pqr + pqi * pqi > 0.0) bt = cdiv_d(-vs->qz_re, -vs->qz_im, pqr, pqi);
+        if (!isfinite(bt.x + bt.y)) bt = make_double2(0.0, 0.0);
+        vs->beta_re = bt.x;
+        vs->beta_im = bt.y;
+        vs->pq_re = vs->pq_im = vs->pr_re = vs->pr_im = vs->qz_re = vs->qz_im = vs->rr = vs->mse = 0.0;
+        vs->counter2 = 0;
+    }
+}
+
+// p = z + beta p
+__global__ void lp_p_kernel(float2* __restrict__ p, const float2* __restrict__ z, long long n, const LpState* st) {
+    if (st->finished) return;
+    const double br = st->beta_re, bi = st->beta_im;
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        const float2 pi = p[i], zi = z[i];
+        p[i] = make_float2((float)((double)zi.x + br * pi.x - bi * pi.y), (float)((double)zi.y + br * pi.y + bi * pi.x));
+    }
+}
+
+// |v|^2 into *out (zeroed by the caller)
+__global__ void lp_norm2_kernel(const float2* __restrict__ v, long long n, double* out) {
+    double s[1] = {0};
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        s[0] += (double)v[i].x * v[i].x + (double)v[i].y * v[i].y;
+    double* const dst[1] = {out};
+    block_accumulate<1>(s, dst);
+}
+
+static unsigned lp_grid(long long n) {
+    return (unsigned)std::max<long long>(1, std::min<long long>(cdiv(n, 256), 2LL * device_sm_count()));
+}
+
+struct LpCall {
+    SenseOp* a;
+    CnnNet* net;
+    int nx, ny, flags;
+    bool has_tik, has_gt;
+};
+
+static void lp_iter(const LpCall& c, LpWorkspace& w, bool learned, cudaStream_t st) {
+    LpState* sp = w.state.as<LpState>();
+    const long long n = w.n;
+    const unsigned g = lp_grid(n);
+    float2* p = w.p.as<float2>();
+    float2* q = w.q.as<float2>();
+    float2* r = w.r.as<float2>();
+    float2* z = learned ? w.z.as<float2>() : r;
+    const float* tik = c.has_tik ? w.tik.as<float>() : nullptr;
+    sense_normal(*c.a, p, q, st, &sp->finished);
+    lp_pq_kernel<<<g, 256, 0, st>>>(p, q, r, tik, n, sp);
+    check_launch("lp_pq");
+    lp_update_kernel<<<g, 256, 0, st>>>(w.x.as<float2>(), p, q, r, c.has_gt ? w.gt.as<float2>() : nullptr, n, sp,
+                                        w.hist.as<double>());
+    check_launch("lp_update");
+    if (learned) cnn_forward(*c.net, r, z, c.nx, c.ny, 1, &sp->rr, c.flags, st);
+    lp_qz_kernel<<<g, 256, 0, st>>>(q, z, n, sp);
+    check_launch("lp_qz");
+    lp_p_kernel<<<g, 256, 0, st>>>(p, z, n, sp);
+    check_launch("lp_p");
+}
+
+static cudaGraphExec_t lp_capture(const LpCall& c, LpWorkspace& w, bool learned, int& kernels) {
+    cudaStream_t st = c.a->stream;
+    MMR_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
+    set_capturing(true);
+    try {
+        lp_iter(c, w, learned, st);
+    } catch (...) {
+        set_capturing(false);
+        cudaGraph_t gr = nullptr;
+        cudaStreamEndCapture(st, &gr);
+        if (gr) cudaGraphDestroy(gr);
+        throw;
+    }
+    set_capturing(false);
+    cudaGraph_t gr = nullptr;
+    MMR_CUDA(cudaStreamEndCapture(st, &gr));
+    size_t nn = 0;
+    MMR_CUDA(cudaGraphGetNodes(gr, nullptr, &nn));
+    std::vector<cudaGraphNode_t> nodes(nn);
+    MMR_CUDA(cudaGraphGetNodes(gr, nodes.data(), &nn));
+    kernels = 0;
+    for (auto nd : nodes) {
+        cudaGraphNodeType t;
+        MMR_CUDA(cudaGraphNodeGetType(nd, &t));
+        if (t == cudaGraphNodeTypeKernel) ++kernels;
+    }
+    cudaGraphExec_t ex = nullptr;
+    cudaError_t e = cudaGraphInstantiate(&ex, gr, 0);
+    cudaGraphDestroy(gr);
+    MMR_CUDA(e);
+    return ex;
+}
+
+// Sets x, r, p (and rr) from scratch: r = b - Hx - tik.*x, z = M(r), p = z.
+static void lp_start(const LpCall& c, LpWorkspace& w, bool learned, bool have_x, bool restart, cudaStream_t st) {
+    LpState* sp = w.state.as<LpState>();
+    const long long n = w.n;
+    const unsigned g = lp_grid(n);
+    MMR_CUDA(cudaMemsetAsync(w.state.p, 0, LP_ACC_BYTES, st));
+    const float2* hx = nullptr;
+    if (have_x) {
+        sense_normal(*c.a, w.x.as<float2>(), w.tmp.as<float2>(), st, nullptr);
+        hx = w.tmp.as<float2>();
+    }
+    lp_init_kernel<<<g, 256, 0, st>>>(w.b.as<float2>(), hx, w.x.as<float2>(), c.has_tik ? w.tik.as<float>() : nullptr,
+                                      c.has_gt ? w.gt.as<float2>() : nullptr, w.r.as<float2>(), n, sp,
+                                      w.hist.as<double>(), restart ? 1 : 0);
+    check_launch("lp_init");
+    if (learned) {
+        cnn_forward(*c.net, w.r.as<float2>(), w.z.as<float2>(), c.nx, c.ny, 1, &sp->rr, c.flags, st);
+        MMR_CUDA(cudaMemcpyAsync(w.p.p, w.z.p, n * 8, cudaMemcpyDeviceToDevice, st));
+    } else {
+        MMR_CUDA(cudaMemcpyAsync(w.p.p, w.r.p, n * 8, cudaMemcpyDeviceToDevice, st));
+    }
+    MMR_CUDA(cudaMemsetAsync(w.state.p, 0, LP_ACC_BYTES, st));
+}
+
+static void lp_solve(SenseOp& a, const void* y_user, CnnNet* net, const void* x0_user, const mmr_lpcg_opts& o,
+                     void* x_user, mmr_lpcg_hist* hist, cudaStream_t ust) {
+    MMR_REQUIRE(a.nufft || a.sho, "operator without a sampling operator");
+    if (!a.lpcg_ws) a.lpcg_ws = new LpWorkspace();
+    LpWorkspace& w = *static_cast<LpWorkspace*>(a.lpcg_ws);
+    const long long n = a.Nimg;
+    const long long nd = a.M * a.C;
+    int nx = 0, ny = 1;
+    if (net) {
+        MMR_REQUIRE(a.nufft && a.nufft->nd == 2, "the learned preconditioner needs a 2D image");
+        nx = a.nufft->N[0];
+        ny = a.nufft->N[1];
+    }
+    w.n = n;
+    for (DevBuf* bb : {&w.x, &w.p, &w.q, &w.r, &w.z, &w.b, &w.tmp}) bb->ensure(n * sizeof(float2));
+    const int nitmax = o.nit_max > 0 ? o.nit_max : 100;
+    const int cap = nitmax + 1;
+    w.state.ensure(sizeof(LpState));
+    w.hist.ensure((size_t)2 * cap * sizeof(double));
+    w.nrm.ensure(2 * sizeof(double));
+    cudaStream_t st = a.stream;
+    cudaEvent_t ev;
+    MMR_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    MMR_CUDA(cudaEventRecord(ev, ust));
+    MMR_CUDA(cudaStreamWaitEvent(st, ev, 0));
+
+    sense_set_weights(a, nullptr, false);
+    const float2* y_in = (const float2*)stage_in(w.sy, y_user, (size_t)nd * 8, st);
+    LpCall c{&a, net, nx, ny, o.flags, o.tik_diag != nullptr || o.lam != 0.0, o.gtruth != nullptr};
+    if (c.has_tik) {
+        w.tik.ensure(n * sizeof(float));
+        std::vector<float> t(n, (float)o.lam);
+        if (o.tik_diag) {
+            std::vector<float> td(n);
+            MMR_CUDA(cudaMemcpy(td.data(), o.tik_diag, n * sizeof(float), cudaMemcpyDefault));
+            for (long long i = 0; i < n; ++i) t[i] += td[i];
+        }
+        MMR_CUDA(cudaMemcpyAsync(w.tik.p, t.data(), n * sizeof(float), cudaMemcpyHostToDevice, st));
+        MMR_CUDA(cudaStreamSynchronize(st));
+    }
+    if (c.has_gt) {
+        w.gt.ensure(n * sizeof(float2));
+        MMR_CUDA(cudaMemcpyAsync(w.gt.p, o.gtruth, n * sizeof(float2), cudaMemcpyDefault, st));
+    }
+    sense_adjoint(a, y_in, w.b.as<float2>(), st, nullptr);
+    if (x0_user) MMR_CUDA(cudaMemcpyAsync(w.x.p, x0_user, n * 8, cudaMemcpyDefault, st));
+    else MMR_CUDA(cudaMemsetAsync(w.x.p, 0, n * 8, st));
+    if (net) cnn_pack(*net, st);
+
+    LpState h = {};
+    h.tol2 = o.tol > 0 ? o.tol * o.tol : 0.0;
+    h.nitmax = nitmax;
+    h.window = o.stall_window;
+    h.cap = cap;
+    h.plain = net ? 0 : 1;
+    MMR_CUDA(cudaMemcpyAsync(w.state.p, &h, sizeof(LpState), cudaMemcpyHostToDevice, st));
+    MMR_CUDA(cudaMemsetAsync(w.hist.p, 0, (size_t)2 * cap * sizeof(double), st));
+    lp_start(c, w, net != nullptr, x0_user != nullptr, false, st);
+
+    const void* key[8] = {a.d_wnorm.p, a.s_grid.p, a.s_grid2.p, w.x.p, w.hist.p, net, net ? net->act.p : nullptr,
+                          net ? net->wmma.p : nullptr};
+    const long long keyv[4] = {a.w_bstride, sense_chunk(a), (n << 2) | ((long long)c.has_tik << 1) | (long long)c.has_gt,
+                               ((long long)o.flags << 32) | (long long)(a.nufft && a.nufft->use_bins ? a.nufft->bins.T : 0)};
+    bool same = w.g_plain != nullptr;
+    for (int i = 0; i < 8 && same; ++i) same = key[i] == w.key[i];
+    for (int i = 0; i < 4 && same; ++i) same = keyv[i] == w.keyv[i];
+    if (!same) {
+        if (w.g_learn) cudaGraphExecDestroy(w.g_learn);
+        if (w.g_plain) cudaGraphExecDestroy(w.g_plain);
+        w.g_learn = w.g_plain = nullptr;
+        w.g_plain = lp_capture(c, w, false, w.k_plain);
+        if (net) w.g_learn = lp_capture(c, w, true, w.k_learn);
+        for (int i = 0; i < 8; ++i) w.key[i] = key[i];
+        for (int i = 0; i < 4; ++i) w.keyv[i] = keyv[i];
+    }
+    bool learned = net != nullptr;
+    int fell_back = -1;
+    const int poll = o.poll > 0 ? o.poll : 8;
+    int it = 0;
+    LpState* sp = w.state.as<LpState>();
+    while (it < nitmax) {
+        const int end = std::min(nitmax, it + poll);
+        for (; it < end; ++it) {
+            MMR_CUDA(cudaGraphLaunch(learned ? w.g_learn : w.g_plain, st));
+            add_launches(learned ? w.k_learn : w.k_plain);
+        }
+        int flags[3] = {0, 0, 0};   // finished, status, stalled
+        MMR_CUDA(cudaMemcpyAsync(flags, &sp->finished, 3 * sizeof(int), cudaMemcpyDeviceToHost, st));
+        MMR_CUDA(cudaStreamSynchronize(st));
+        if (flags[0]) break;
+        if (learned && flags[2]) {
+            // the true residual stopped falling: restart plain CG from the current x
+            int nit = 0;
+            MMR_CUDA(cudaMemcpy(&nit, &sp->nit, sizeof(int), cudaMemcpyDeviceToHost));
+            fell_back = nit;
+            learned = false;
+            const int one = 1, zero = 0;
+            MMR_CUDA(cudaMemcpyAsync(&sp->plain, &one, sizeof(int), cudaMemcpyHostToDevice, st));
+            MMR_CUDA(cudaMemcpyAsync(&sp->stalled, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
+            lp_start(c, w, false, true, true, st);
+            MMR_CUDA(cudaStreamSynchronize(st));
+        }
+    }
+    // judge: true residual |b - Hx - tik.*x| / |b|
+    sense_normal(a, w.x.as<float2>(), w.tmp.as<float2>(), st, nullptr);
+    MMR_CUDA(cudaMemsetAsync(w.state.p, 0, LP_ACC_BYTES, st));
+    lp_init_kernel<<<lp_grid(n), 256, 0, st>>>(w.b.as<float2>(), w.tmp.as<float2>(), w.x.as<float2>(),
+                                               c.has_tik ? w.tik.as<float>() : nullptr, nullptr, w.q.as<float2>(), n,
+                                               sp, w.hist.as<double>(), 1);
+    check_launch("lp_init");
+    MMR_CUDA(cudaMemsetAsync(w.nrm.p, 0, 2 * sizeof(double), st));
+    lp_norm2_kernel<<<lp_grid(n), 256, 0, st>>>(w.b.as<float2>(), n, w.nrm.as<double>());
+    check_launch("lp_norm2");
+    LpState fs;
+    double bn = 0;
+    MMR_CUDA(cudaMemcpyAsync(&fs, sp, sizeof(LpState), cudaMemcpyDeviceToHost, st));
+    MMR_CUDA(cudaMemcpyAsync(&bn, w.nrm.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+    float2* xo = (float2*)stage_out(w.sxo, x_user, n * 8);
+    MMR_CUDA(cudaMemcpyAsync(xo, w.x.p, n * 8, cudaMemcpyDeviceToDevice, st));
+    finish_out(w.sxo, n * 8, st);
+    MMR_CUDA(cudaStreamSynchronize(st));
+    if (hist) {
+        hist->nit = fs.nit;
+        hist->n = std::min(cap, fs.nit + 1);
+        hist->status = fs.status;
+        hist->fell_back_at = fell_back;
+        hist->true_res_rel = bn > 0 ? std::sqrt(fs.rr / bn) : 0.0;
+        std::vector<double> hh((size_t)2 * cap);
+        MMR_CUDA(cudaMemcpy(hh.data(), w.hist.p, hh.size() * sizeof(double), cudaMemcpyDeviceToHost));
+        const int m = std::min(hist->capacity, hist->n);
+        for (int i = 0; i < m; ++i) {
+            if (hist->res_sq) hist->res_sq[i] = hh[i];
+            if (hist->err_sq) hist->err_sq[i] = hh[cap + i];
+        }
+    }
+    MMR_CUDA(cudaEventRecord(ev, st));
+    MMR_CUDA(cudaStreamWaitEvent(ust, ev, 0));
+    cudaEventDestroy(ev);
+}
+
+}  // namespace mmr
+
+using namespace mmr;
+
+extern "C" int mmr_lpcg_default_opts(mmr_lpcg_opts* o) {
+    return guarded([&] {
+        MMR_REQUIRE(o, "NULL opts");
+        memset(o, 0, sizeof(*o));
+        o->nit_max = 100;
+        o->tol = 0.0;
+        o->stall_window = 5;
+        o->flags = 2;   // tensor-core network forward
+        o->poll = 8;
+    });
+}
+
+extern "C" int mmr_lpcg_solve(mmr_sense* A, const void* y, mmr_cnn* net, const void* x0, const mmr_lpcg_opts* opts,
+                              void* x_out, mmr_lpcg_hist* hist, void* stream) {
+    return guarded([&] {
+        MMR_REQUIRE(A && y && x_out, "NULL argument");
+        mmr_lpcg_opts o;
+        if (opts) o = *opts;
+        else mmr_lpcg_default_opts(&o);
+        lp_solve(A->a, y, net ? &net->n : nullptr, x0, o, x_out, hist, as_stream(stream));
+    });
+}

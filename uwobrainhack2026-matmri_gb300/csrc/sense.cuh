@@ -51,6 +51,7 @@ struct SenseOp {
     Staged st_in, st_out;
     cudaStream_t stream = nullptr;       // internal non-blocking stream (graphs)
     void* solver_ws = nullptr;           // cg workspace (cg.cu)
+    void* lpcg_ws = nullptr;             // learned-PCG workspace (lpcg.cu)
 };
 
 int sense_chunk(const SenseOp& a);
@@ -62,7 +63,9 @@ void sense_adjoint(SenseOp& a, const float2* y, float2* x, cudaStream_t st, cons
 // normal op A^H diag(d_wnorm) A (+ tikreg^2) x
 void sense_normal(SenseOp& a, const float2* x, float2* y, cudaStream_t st, const int* active);
 
+// Frees the solver workspaces and their CUDA graphs (cg and learned PCG).
 void cg_release(SenseOp& a);
+void lpcg_release(SenseOp& a);
 
 }  // namespace mmr
 

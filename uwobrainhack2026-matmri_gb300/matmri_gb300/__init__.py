@@ -10,6 +10,7 @@ from ._lib import MatmriError, load as load_library
 from .ops import nufftOp, rcvrOp, sampHighOrder
 from .sense import mrSampFunc, mrSampOp
 from .solvers import bfista, cgne, dwtND, powermethod
+from .learned import PrecondNet, lpcg
 
 __all__ = ["nufftOp", "rcvrOp", "sampHighOrder", "mrSampFunc", "mrSampOp", "cgne", "powermethod", "bfista",
-           "dwtND", "MatmriError", "load_library"]
+           "dwtND", "PrecondNet", "lpcg", "MatmriError", "load_library"]

@@ -75,6 +75,21 @@ class BfistaHist(C.Structure):
                 ("max_eig", C.c_double)]
 
 
+class LpcgOpts(C.Structure):
+    _fields_ = [("nit_max", C.c_int32), ("tol", C.c_double), ("tik_diag", C.POINTER(C.c_float)),
+                ("lam", C.c_double), ("gtruth", C.c_void_p), ("stall_window", C.c_int32), ("flags", C.c_int32),
+                ("poll", C.c_int32)]
+
+
+class LpcgHist(C.Structure):
+    _fields_ = [("res_sq", C.POINTER(C.c_double)), ("err_sq", C.POINTER(C.c_double)), ("capacity", C.c_int32),
+                ("n", C.c_int32), ("nit", C.c_int32), ("status", C.c_int32), ("fell_back_at", C.c_int32),
+                ("true_res_rel", C.c_double)]
+
+
+CNN_FP32_ACT = 1
+CNN_TENSOR = 2
+
 # name -> (restype, argtypes)
 SIGNATURES = {
     "mmr_abi_version": (C.c_int, []),
@@ -112,6 +127,19 @@ SIGNATURES = {
     "mmr_bfista_solve": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_float), C.c_int32,
                                    C.c_void_p, C.POINTER(BfistaOpts), C.c_void_p, C.POINTER(BfistaHist),
                                    C.c_void_p]),
+    "mmr_cnn_create": (C.c_int, [C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_void_p)]),
+    "mmr_cnn_num_params": (C.c_int, [C.c_void_p, C.POINTER(C.c_int64)]),
+    "mmr_cnn_set_params": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "mmr_cnn_get_params": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "mmr_cnn_forward": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_int32,
+                                  C.c_void_p]),
+    "mmr_cnn_loss_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_int32,
+                                    C.c_int32, C.POINTER(C.c_double), C.c_void_p, C.c_void_p]),
+    "mmr_cnn_adam_step": (C.c_int, [C.c_void_p, C.c_float, C.c_void_p]),
+    "mmr_cnn_destroy": (C.c_int, [C.c_void_p]),
+    "mmr_lpcg_default_opts": (C.c_int, [C.POINTER(LpcgOpts)]),
+    "mmr_lpcg_solve": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(LpcgOpts), C.c_void_p,
+                                 C.POINTER(LpcgHist), C.c_void_p]),
 }
 
 _lib = None

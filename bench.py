@@ -148,6 +148,138 @@ def cpu_baseline(case, reps=2):
                       f"operators per solve; {t_norm:.3f} s per normal operator"}
 
 
+LEARNED_SEED = 5000          # held out: training seeds start at 100000, validation at 200000
+NRMSE_TARGET = 1e-3
+
+
+def learned_pcg_comparison(dev, reps=5):
+    """Time to NRMSE <= 1e-3 against the converged image: learned-PCG vs plain CG.
+
+    Workload: 256 x 256, 32 randomised coil maps, 4 x 4096 spiral R = 4, SNR 30, the
+    Tikhonov-regularised system the preconditioner was trained for ((A'A + lam) x = A'y, cgne with
+    gam = lam, R = 1).  The converged image is plain CG run 300 + 100 iterations (its drift over the
+    last 100 is reported).  Iteration counts come from the error histories (opt.gtruth); the times are
+    then taken for solves of exactly that many iterations from device-resident data.
+    """
+    import torch
+    import matmri_gb300 as mm
+    from matmri_gb300 import synth
+    from matmri_gb300.learned import PrecondNet, iterations_to, lpcg
+    from matmri_gb300 import train_precond as tp
+    if not os.path.exists(tp.WEIGHTS):
+        return {"unavailable": "no trained weights at " + os.path.relpath(tp.WEIGHTS, ROOT)}
+    meta = np.load(tp.WEIGHTS)
+    lam = float(meta["lam"])
+    net = PrecondNet.load(tp.WEIGHTS)
+    c = synth.sense_case(N_IMG, N_COIL, N_INT, N_SAMP, ACCEL, seed=LEARNED_SEED, randomize_coils=True)
+    S = mm.nufftOp([N_IMG, N_IMG], c["kloc"], None, 1, 2.0, 4)
+    R = mm.rcvrOp(c["maps"], 0)
+    A = mm.mrSampOp(S, R)
+    y = np.asarray(A(c["img"].astype(np.complex64), "notransp"), dtype=np.complex128)
+    y = synth.add_noise(y, 30.0, LEARNED_SEED + 7).astype(np.complex64)
+    yd = torch.from_numpy(np.ascontiguousarray(y.T)).to(dev).T
+    xs, _, _, _ = lpcg(A, yd, None, NitMax=300, lam=lam)
+    xs2, _, _, _ = lpcg(A, yd, None, x0=xs, NitMax=100, lam=lam)
+    drift = float(torch.linalg.norm(xs2 - xs) / torch.linalg.norm(xs2))
+    xs = xs2
+    gn = float(torch.linalg.norm(xs))
+    zeros = torch.zeros_like(xs)
+    opt = {"resThresh": None, "xChangeThresh": None}
+    _, _, mse, _, _, _, _ = mm.cgne(A, yd, zeros, 150, dict(opt, gtruth=xs), lam, 1.0)
+    k_cgne = iterations_to(mse, gn, NRMSE_TARGET)
+    _, _, err_p, _ = lpcg(A, yd, None, NitMax=150, lam=lam, gtruth=xs)
+    k_plain = iterations_to(err_p, gn, NRMSE_TARGET)
+    _, _, err_l, info = lpcg(A, yd, net, NitMax=150, lam=lam, gtruth=xs)
+    k_learn = iterations_to(err_l, gn, NRMSE_TARGET)
+    if None in (k_cgne, k_plain, k_learn):
+        return {"unavailable": f"target not reached within 150 iterations (cgne {k_cgne}, plain {k_plain}, "
+                               f"learned {k_learn})"}
+    st = torch.cuda.current_stream(dev)
+
+    def timed(fn):
+        for _ in range(2):
+            fn()
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(st)
+            fn()
+            e1.record(st)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return statistics.median(ts)
+
+    t_cgne = timed(lambda: mm.cgne(A, yd, zeros, k_cgne, opt, lam, 1.0))
+    t_plain = timed(lambda: lpcg(A, yd, None, NitMax=k_plain, lam=lam))
+    x_l = None
+
+    def run_learned():
+        nonlocal x_l
+        x_l, _, _, _ = lpcg(A, yd, net, NitMax=k_learn, lam=lam)
+
+    t_learn = timed(run_learned)
+    nrmse_l = float(torch.linalg.norm(x_l - xs)) / gn
+    t_plain_best = min(t_cgne, t_plain)
+    return {"workload": "cg-sense 256x256, 32 randomised coils, 4x4096 spiral R=4, SNR 30, Tikhonov lam = "
+                        f"{float(meta['lam_rel']):g} lambda_max(A'A), x0 = 0, seed {LEARNED_SEED} (held out)",
+            "nrmse_target": NRMSE_TARGET, "reference_drift": drift,
+            "plain_cgne_iters": k_cgne, "plain_cgne_ms": t_cgne,
+            "plain_fcg_iters": k_plain, "plain_fcg_ms": t_plain,
+            "learned_iters": k_learn, "learned_ms": t_learn, "learned_nrmse": nrmse_l,
+            "learned_fell_back_at": info["fell_back_at"], "learned_true_res_rel": info["true_res_rel"],
+            "time_ratio_vs_best_plain": t_learn / t_plain_best, "network": os.path.relpath(tp.WEIGHTS, ROOT)}
+
+
+def batched_comparison(dev, nit=25, reps=3):
+    """64 uneven CG-SENSE slices (N in {96,128,192,256}, C in {8,16,32}, 2-8 interleaves x 2048-4096
+    samples, own spiral each), cgne with 25 iterations each: the batch advanced by one CUDA graph per
+    iteration (every slice a parallel branch; launch shapes autotuned once per (N, C) class) against
+    the same 64 solves issued one after another."""
+    import torch
+    import matmri_gb300 as mm
+    from matmri_gb300 import synth
+    from matmri_gb300.autotune import autotune
+    cases = synth.batched_cases(64)
+    ops, ys, classes = [], [], {}
+    t0 = time.perf_counter()
+    for c in cases:
+        N = c["N"]
+        A = mm.mrSampOp(mm.nufftOp([N, N], c["kloc"], None, 1, 2.0, 4), mm.rcvrOp(c["maps"], 0))
+        y = np.asarray(A(c["img"].astype(np.complex64), "notransp"))
+        ys.append(torch.from_numpy(np.ascontiguousarray(y.T)).to(dev).T)
+        key = (N, c["C"])
+        if key not in classes:
+            classes[key] = autotune(A, rounds=1, use_cache=False)
+        else:
+            A.set_tuning(**classes[key])
+        ops.append(A)
+    setup_s = time.perf_counter() - t0
+    opt = {"resThresh": None, "xChangeThresh": None}
+    st = torch.cuda.current_stream(dev)
+
+    def timed(fn):
+        fn()
+        ts = []
+        for _ in range(reps):
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            e0.record(st)
+            fn()
+            e1.record(st)
+            torch.cuda.synchronize()
+            ts.append(e0.elapsed_time(e1))
+        return statistics.median(ts)
+
+    t_batch = timed(lambda: mm.cgne_batch(ops, ys, nit, opt))
+    t_seq = timed(lambda: [mm.cgne(A, y, None, nit, opt) for A, y in zip(ops, ys)])
+    return {"workload": "64 uneven cg-sense slices, N in {96,128,192,256}, C in {8,16,32}, 2-8 interleaves x "
+                        f"2048-4096 samples, {nit} cgne iterations each, kwidth 4, os 2",
+            "slices": len(ops), "size_classes": len(classes), "batched_ms": t_batch, "sequential_ms": t_seq,
+            "slices_per_s": len(ops) / (t_batch / 1e3), "speedup_vs_sequential": t_seq / t_batch,
+            "setup_s": setup_s}
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -191,6 +323,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned-PCG vs plain-CG comparison")
+    ap.add_argument("--no-batched", action="store_true", help="skip the 64-slice batched comparison")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--tuning", default=None,
                     help="fixed knobs coil_chunk,tile,coil_group,item,fft_lines,normal_mode (skips the autotuner)")
@@ -351,6 +485,10 @@ def main():
                                          "frac": value * solve_bytes / 1e9 / peak}},
             "clocks": clk.summary(),
         }
+        if not args.no_learned:
+            line["learned_pcg"] = learned_pcg_comparison(dev)
+        if not args.no_batched:
+            line["batched"] = batched_comparison(dev)
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(case)
         print(json.dumps(line), flush=True)

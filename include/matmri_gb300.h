@@ -247,6 +247,15 @@ MMR_API int mmr_cgne_solve(mmr_sense* A, const void* b, const void* x0, const fl
                    const mmr_cgne_opts* opts, void* x_out, mmr_cgne_hist* hist,
                    void* stream);
 
+/* n independent cgne solves (e.g. slices with different matrix sizes, coil
+ * counts and trajectories: one mmr_sense each, all distinct) run together:
+ * one CUDA graph holds one iteration of every solve as parallel branches, so
+ * each graph launch advances the whole batch (a loop over cgne calls in the
+ * reference).  Same options for all (x0 = A'b, no W); stopping rules act per
+ * solve; hists may be NULL or an array of n.                               */
+MMR_API int mmr_cgne_solve_batch(mmr_sense* const* A, int32_t n, const void* const* b, void* const* x_out,
+                                 const mmr_cgne_opts* opts, mmr_cgne_hist* hists, void* stream);
+
 /* ---- powermethod / bfista --------------------------------------------------
  * powermethod(A, x0, NitMax, doAtA=1, xdiffThresh)  (iterativeSolvers/powermethod.m:1-67) */
 MMR_API int mmr_powermethod(mmr_sense* A, const void* x0, int32_t nit_max, double xdiff_thresh,
@@ -300,6 +309,10 @@ typedef struct mmr_cnn mmr_cnn;
 
 #define MMR_CNN_FP32_ACT 1   /* keep activations in FP32 (default BF16)       */
 #define MMR_CNN_TENSOR   2   /* tensor-core forward of the hidden layers      */
+#define MMR_CNN_LOSS_COS 4   /* loss_grad: 1 - |<z,e>|^2/(|z|^2 |e|^2) instead of
+                                the relative L2 (invariant to a complex scale)  */
+#define MMR_CNN_LINEAR   8   /* identity activations: the network is a fixed
+                                linear operator (forward and loss_grad)       */
 
 MMR_API int mmr_cnn_create(int32_t nlayers, const int32_t* channels, mmr_cnn** out);
 MMR_API int mmr_cnn_num_params(const mmr_cnn* net, int64_t* n);
@@ -310,8 +323,9 @@ MMR_API int mmr_cnn_get_params(const mmr_cnn* net, float* theta);
 MMR_API int mmr_cnn_forward(mmr_cnn* net, const void* r, void* z, int64_t nx, int64_t ny, int64_t batch,
                             int32_t flags, void* stream);
 /* Loss L = mean_b |m.*(net(r_b) - e_b)|^2 / |m.*e_b|^2 (m: the interior
- * mask without `margin` pixels on each side) and dL/dtheta, kept on the
- * device for mmr_cnn_adam_step and copied to `grad` (host, may be NULL). */
+ * mask without `margin` pixels on each side; MMR_CNN_LOSS_COS selects
+ * mean_b 1 - |<m z_b, m e_b>|^2 / (|m z_b|^2 |m e_b|^2)) and dL/dtheta, kept
+ * on the device for mmr_cnn_adam_step and copied to `grad` (host, or NULL). */
 MMR_API int mmr_cnn_loss_grad(mmr_cnn* net, const void* r, const void* e, int64_t nx, int64_t ny, int64_t batch,
                               int32_t margin, int32_t flags, double* loss, float* grad, void* stream);
 /* One Adam step (beta1 0.9, beta2 0.999, eps 1e-8) with the last gradient. */
@@ -330,7 +344,7 @@ typedef struct mmr_lpcg_opts {
     const float*  tik_diag;      /* optional [imN] real diagonal T (host/device)  */
     double        lam;           /* scalar added to T (Tikhonov gam with R = 1)   */
     const void*   gtruth;        /* optional [imN] complex64 for the error history */
-    int32_t       stall_window;  /* fallback window (default 5; 0 = never)        */
+    int32_t       stall_window;  /* fallback window (default 10; 0 = never)       */
     int32_t       flags;         /* MMR_CNN_* network flags (default TENSOR)      */
     int32_t       poll;          /* host checks the device flags every poll its (8) */
 } mmr_lpcg_opts;

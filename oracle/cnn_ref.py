@@ -12,6 +12,7 @@ Network (complex image in, complex image out, 2 real channels):
   s  = sqrt(mean |r|^2)                 (per image; s = 0 gives z = 0)
   a0 = [re(r), im(r)] / s
   a_{l+1} = relu(conv3x3(a_l, W_l))     l = 0..4, channels 2->32->32->32->32->32
+                                        (identity instead of relu when linear=True)
   v  = conv3x3(a_5, W_5) + skip * a0    32 -> 2
   z  = s * (v[0] + i v[1])
 conv3x3: zero padding, stride 1, no bias, cross-correlation
@@ -89,7 +90,7 @@ def _planes(r):
     return a0, s
 
 
-def forward(theta, r, channels=CHANNELS, keep=False):
+def forward(theta, r, channels=CHANNELS, keep=False, linear=False):
     """z = net(r) for r [B, X, Y] complex; returns z [B, X, Y] (and the activations if keep)."""
     Ws, skip = unpack(theta, channels)
     a0, s = _planes(r)
@@ -97,7 +98,7 @@ def forward(theta, r, channels=CHANNELS, keep=False):
     a = a0
     for l, W in enumerate(Ws):
         pre = conv3x3(a, W)
-        a = np.maximum(pre, 0.0) if l < len(Ws) - 1 else pre
+        a = np.maximum(pre, 0.0) if (l < len(Ws) - 1 and not linear) else pre
         acts.append(a)
     v = a + skip * a0
     zt = v.transpose(0, 1, 3, 2)
@@ -107,20 +108,35 @@ def forward(theta, r, channels=CHANNELS, keep=False):
     return z
 
 
-def loss_and_grad(theta, r, e, margin, channels=CHANNELS):
-    """L = mean_b ||m (z_b - e_b)||^2 / ||m e_b||^2 with m the interior mask (margin pixels
-    dropped on every side); returns (L, dL/dtheta)."""
+def loss_and_grad(theta, r, e, margin, channels=CHANNELS, kind="rel", linear=False):
+    """Loss over the interior mask m (margin pixels dropped on every side) and dL/dtheta.
+
+    kind "rel": L = mean_b ||m (z_b - e_b)||^2 / ||m e_b||^2
+    kind "cos": L = mean_b 1 - |<m z_b, m e_b>|^2 / (||m z_b||^2 ||m e_b||^2), invariant to a complex
+                scale of z_b (flexible CG's line search fixes the scale of each direction).
+    """
     Ws, skip = unpack(theta, channels)
-    z, acts, s = forward(theta, r, channels, keep=True)
+    z, acts, s = forward(theta, r, channels, keep=True, linear=linear)
     B, X, Y = z.shape
     m = np.zeros((X, Y))
     m[margin:X - margin, margin:Y - margin] = 1.0
     e = np.asarray(e, dtype=np.complex128)
     den = np.sum(m * np.abs(e) ** 2, axis=(1, 2))
     den = np.where(den > 0, den, 1.0)
-    diff = m * (z - e)
-    L = float(np.mean(np.sum(np.abs(diff) ** 2, axis=(1, 2)) / den))
-    gz = 2.0 * diff / den[:, None, None] / B                         # dL/d(re z) + i dL/d(im z)
+    if kind == "rel":
+        diff = m * (z - e)
+        L = float(np.mean(np.sum(np.abs(diff) ** 2, axis=(1, 2)) / den))
+        gz = 2.0 * diff / den[:, None, None] / B                     # dL/d(re z) + i dL/d(im z)
+    else:
+        zm, em = m * z, m * e
+        Z = np.sum(np.abs(zm) ** 2, axis=(1, 2))
+        c = np.sum(np.conj(zm) * em, axis=(1, 2))
+        ok = Z > 0
+        Zs = np.where(ok, Z, 1.0)
+        L = float(np.mean(np.where(ok, 1.0 - np.abs(c) ** 2 / (Zs * den), 1.0)))
+        gz = (-2.0 * np.conj(c)[:, None, None] * em / (Zs * den)[:, None, None]
+              + 2.0 * (np.abs(c) ** 2)[:, None, None] * zm / (Zs ** 2 * den)[:, None, None]) / B
+        gz = np.where(ok[:, None, None], gz, 0.0)
     gv = np.stack([gz.real, gz.imag], axis=1).transpose(0, 1, 3, 2) * s[:, None, None, None]
     grads = [None] * len(Ws)
     dskip = float(np.sum(gv * acts[0]))
@@ -128,7 +144,9 @@ def loss_and_grad(theta, r, e, margin, channels=CHANNELS):
     for l in range(len(Ws) - 1, -1, -1):
         grads[l] = conv3x3_wgrad(acts[l], g)
         if l > 0:
-            g = conv3x3_dgrad(g, Ws[l]) * (acts[l] > 0)
+            g = conv3x3_dgrad(g, Ws[l])
+            if not linear:
+                g = g * (acts[l] > 0)
     flat = np.concatenate([gw.reshape(-1) for gw in grads] + [np.array([dskip])])
     return L, flat
 

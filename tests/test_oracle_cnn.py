@@ -60,3 +60,25 @@ def test_adam_step_matches_closed_form_first_step():
     # first step moves each nonzero-gradient weight by lr * sign(g)
     np.testing.assert_allclose(t2[:2], th[:2] - 0.01 * np.sign(gr[:2]), rtol=1e-6)
     assert t2[2] == th[2]
+
+
+def test_cosine_loss_gradient_and_scale_invariance():
+    ch = (2, 4, 3, 2)
+    g = np.random.Generator(np.random.PCG64(8))
+    theta = cnn_ref.init_params(9, ch).astype(np.float64)
+    theta[-1] = 0.2
+    r = _rand_c(g, 2, 9, 8)
+    e = _rand_c(g, 2, 9, 8)
+    L, grad = cnn_ref.loss_and_grad(theta, r, e, 1, ch, kind="cos")
+    assert 0.0 <= L <= 1.0
+    for i in list(g.choice(len(theta) - 1, 20, replace=False)) + [len(theta) - 1]:
+        h = 1e-6
+        tp, tm = theta.copy(), theta.copy()
+        tp[i] += h
+        tm[i] -= h
+        fd = (cnn_ref.loss_and_grad(tp, r, e, 1, ch, kind="cos")[0]
+              - cnn_ref.loss_and_grad(tm, r, e, 1, ch, kind="cos")[0]) / (2 * h)
+        assert abs(fd - grad[i]) <= 1e-6 * max(1.0, abs(fd)), (i, fd, grad[i])
+    # a complex rescaling of the target leaves the loss unchanged
+    L2, _ = cnn_ref.loss_and_grad(theta, r, (2 - 3j) * e, 1, ch, kind="cos")
+    assert abs(L2 - L) < 1e-12

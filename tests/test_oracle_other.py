@@ -127,3 +127,15 @@ def test_bfista_decreases_cost():
     x, rs, rx, test, me = bfista_ref(f, b, HaarRef([1, 1], [8, 8]), 0.1, x0, 30, {"resThresh": 0})
     cost = rs + rx
     assert cost[-1] < cost[0]
+
+
+def test_torch_generators_match_numpy():
+    torch = pytest.importorskip("torch")
+    from matmri_gb300 import synth
+    img = synth.ellipse_phantom(48, 10, 7, complex_phase=True)
+    it = synth.ellipse_phantom_torch(48, 10, 7, complex_phase=True, device="cpu").numpy()
+    assert np.abs(it - img).max() < 1e-6
+    m = synth.coil_maps(40, 6, 3, randomize=True)
+    mt = synth.coil_maps_torch(40, 6, 3, randomize=True, device="cpu")
+    assert mt.shape == (40, 40, 6) and mt.stride() == (1, 40, 1600)
+    assert np.abs(mt.numpy() - m).max() < 1e-6

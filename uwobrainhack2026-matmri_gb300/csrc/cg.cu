@@ -278,10 +278,8 @@ static unsigned red_grid(long long n) {
 
 static bool isset(double v) { return !std::isnan(v); }
 
-// Captures one iteration (explicit or not) on `st`.
-static cudaGraphExec_t capture_iter(SenseOp& a, CgWorkspace& w, bool expl, bool has_tik, bool has_gt,
-                                    int& kernels) {
-    cudaStream_t st = a.stream;
+// The kernels of one iteration (explicit residual or not) of the solve in `w`, issued on `st`.
+static void iter_body(SenseOp& a, CgWorkspace& w, bool expl, bool has_tik, bool has_gt, cudaStream_t st) {
     CgState* sp = w.state.as<CgState>();
     double* hist = w.hist.as<double>();
     const long long n = w.n;
@@ -293,19 +291,27 @@ static cudaGraphExec_t capture_iter(SenseOp& a, CgWorkspace& w, bool expl, bool 
     float2* Ap = w.Ap.as<float2>();
     const float* tik = has_tik ? w.tik.as<float>() : nullptr;
     const float2* gt = has_gt ? w.gt.as<float2>() : nullptr;
+    sense_normal(a, p, Ap, st, active);
+    cg_pap_kernel<<<g, 256, 0, st>>>(p, Ap, tik, n, sp);
+    if (expl) {
+        cg_update_kernel<1><<<g, 256, 0, st>>>(x, p, Ap, res, gt, n, sp, hist);
+        sense_normal(a, x, w.tmp.as<float2>(), st, active);
+        cg_res_explicit_kernel<<<g, 256, 0, st>>>(w.b.as<float2>(), w.tmp.as<float2>(), x, tik, res, n, sp, hist);
+    } else {
+        cg_update_kernel<0><<<g, 256, 0, st>>>(x, p, Ap, res, gt, n, sp, hist);
+    }
+    cg_p_kernel<<<g, 256, 0, st>>>(p, res, n, sp);
+}
+
+static cudaGraphExec_t instantiate_counted(cudaGraph_t gr, int& kernels);
+
+// Captures `body` (issued on `st`) as a graph; the capture is closed on every error path.
+template <class F>
+static cudaGraphExec_t capture(cudaStream_t st, F&& body, int& kernels) {
     MMR_CUDA(cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed));
     set_capturing(true);
     try {
-        sense_normal(a, p, Ap, st, active);
-        cg_pap_kernel<<<g, 256, 0, st>>>(p, Ap, tik, n, sp);
-        if (expl) {
-            cg_update_kernel<1><<<g, 256, 0, st>>>(x, p, Ap, res, gt, n, sp, hist);
-            sense_normal(a, x, w.tmp.as<float2>(), st, active);
-            cg_res_explicit_kernel<<<g, 256, 0, st>>>(w.b.as<float2>(), w.tmp.as<float2>(), x, tik, res, n, sp, hist);
-        } else {
-            cg_update_kernel<0><<<g, 256, 0, st>>>(x, p, Ap, res, gt, n, sp, hist);
-        }
-        cg_p_kernel<<<g, 256, 0, st>>>(p, res, n, sp);
+        body();
     } catch (...) {
         set_capturing(false);
         cudaGraph_t gr = nullptr;
@@ -316,6 +322,17 @@ static cudaGraphExec_t capture_iter(SenseOp& a, CgWorkspace& w, bool expl, bool 
     set_capturing(false);
     cudaGraph_t gr = nullptr;
     MMR_CUDA(cudaStreamEndCapture(st, &gr));
+    return instantiate_counted(gr, kernels);
+}
+
+// Captures one iteration (explicit or not) on the operator's stream.
+static cudaGraphExec_t capture_iter(SenseOp& a, CgWorkspace& w, bool expl, bool has_tik, bool has_gt,
+                                    int& kernels) {
+    return capture(a.stream, [&] { iter_body(a, w, expl, has_tik, has_gt, a.stream); }, kernels);
+}
+
+// Instantiates `gr` (destroyed here) and counts its kernel nodes.
+static cudaGraphExec_t instantiate_counted(cudaGraph_t gr, int& kernels) {
     size_t nn = 0;
     MMR_CUDA(cudaGraphGetNodes(gr, nullptr, &nn));
     std::vector<cudaGraphNode_t> nodes(nn);
@@ -333,8 +350,19 @@ static cudaGraphExec_t capture_iter(SenseOp& a, CgWorkspace& w, bool expl, bool 
     return ex;
 }
 
-static void cg_solve(SenseOp& a, const void* b_user, const void* x0_user, const float* W, const mmr_cgne_opts& o,
-                     void* x_user, mmr_cgne_hist* hist, cudaStream_t ust) {
+// What one solve needs between its set-up and its read-back.
+struct CgRun {
+    int nitmax0 = 0, extra = 0, cap = 0, expResN = 1, limit = 0;
+    bool has_tik = false, has_gt = false, has_stop = false, dynamic = false;
+    double stop_thresh_out = NAN;
+    cudaEvent_t ev = nullptr;
+};
+
+// Set-up of one solve on the operator's stream (ordered after `ust`): inputs, b = A'(W.*y),
+// x0, the options in the device state, the initial residual (cgne.m:135-207).
+static CgRun cg_begin(SenseOp& a, const void* b_user, const void* x0_user, const float* W, const mmr_cgne_opts& o,
+                      cudaStream_t ust) {
+    CgRun run;
     if (!a.solver_ws) a.solver_ws = new CgWorkspace();
     CgWorkspace& w = *static_cast<CgWorkspace*>(a.solver_ws);
     const long long n = a.Nimg;
@@ -350,6 +378,7 @@ static void cg_solve(SenseOp& a, const void* b_user, const void* x0_user, const 
     // order the internal stream after the caller's stream
     cudaEvent_t ev;
     MMR_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    run.ev = ev;
     MMR_CUDA(cudaEventRecord(ev, ust));
     MMR_CUDA(cudaStreamWaitEvent(st, ev, 0));
 
@@ -426,42 +455,28 @@ static void cg_solve(SenseOp& a, const void* b_user, const void* x0_user, const 
                                                has_gt ? w.gt.as<float2>() : nullptr, w.res.as<float2>(),
                                                w.p.as<float2>(), n, sp, w.hist.as<double>());
     check_launch("cg_init");
+    run.nitmax0 = nitmax0;
+    run.extra = extra;
+    run.cap = cap;
+    run.expResN = std::max(1, o.exp_res_n);
+    run.has_tik = has_tik;
+    run.has_gt = has_gt;
+    run.has_stop = h.has_stop;
+    run.stop_thresh_out = stop_thresh_out;
+    run.dynamic = h.has_resThresh || h.has_resChange || h.has_xChange || h.has_stop || h.stopOnResInc > 0 ||
+                  h.stopOnXdifInc > 0;
+    run.limit = nitmax0 + (h.has_stop ? extra : 0);
+    return run;
+}
 
-    // graphs (re-captured when buffers or options that change kernel arguments differ)
-    const void* key[8] = {a.d_wnorm.p, a.s_grid.p, a.s_grid2.p, w.x.p, w.hist.p, (const void*)(intptr_t)has_tik,
-                          (const void*)(intptr_t)has_gt, a.nufft ? a.nufft->s_tmp.p : nullptr};
-    const long long keyv[4] = {a.w_bstride, sense_chunk(a), a.nufft && a.nufft->use_bins ? a.nufft->bins.T : 0, cap};
-    bool same = w.g_norm != nullptr;
-    for (int i = 0; i < 8 && same; ++i) same = key[i] == w.key[i];
-    for (int i = 0; i < 4 && same; ++i) same = keyv[i] == w.keyv[i];
-    if (!same) {
-        if (w.g_norm) cudaGraphExecDestroy(w.g_norm);
-        if (w.g_expl) cudaGraphExecDestroy(w.g_expl);
-        w.g_norm = w.g_expl = nullptr;
-        // one eager normal op sizes every scratch buffer before capture
-        w.g_norm = capture_iter(a, w, false, has_tik, has_gt, w.k_norm);
-        w.g_expl = capture_iter(a, w, true, has_tik, has_gt, w.k_expl);
-        for (int i = 0; i < 8; ++i) w.key[i] = key[i];
-        for (int i = 0; i < 4; ++i) w.keyv[i] = keyv[i];
-    }
-    const int expResN = std::max(1, o.exp_res_n);
-    const bool dynamic = h.has_resThresh || h.has_resChange || h.has_xChange || h.has_stop || h.stopOnResInc > 0 ||
-                         h.stopOnXdifInc > 0;
-    const int limit = nitmax0 + (h.has_stop ? extra : 0);
-    const int poll = dynamic ? 4 : limit;
-    int it = 0;
-    while (it < limit) {
-        const int end = std::min(limit, it + poll);
-        for (; it < end; ++it) {
-            const bool ex = it % expResN == 0;
-            MMR_CUDA(cudaGraphLaunch(ex ? w.g_expl : w.g_norm, st));
-            add_launches(ex ? w.k_expl : w.k_norm);
-        }
-        int fin = 0;
-        MMR_CUDA(cudaMemcpyAsync(&fin, &sp->finished, sizeof(int), cudaMemcpyDeviceToHost, st));
-        MMR_CUDA(cudaStreamSynchronize(st));
-        if (fin) break;
-    }
+// Read-back of one solve: x, histories, status (cgne.m:336-340); releases the run's event.
+static void cg_end(SenseOp& a, CgRun& run, void* x_user, mmr_cgne_hist* hist, cudaStream_t ust) {
+    CgWorkspace& w = *static_cast<CgWorkspace*>(a.solver_ws);
+    cudaStream_t st = a.stream;
+    CgState* sp = w.state.as<CgState>();
+    const long long n = w.n;
+    const int cap = run.cap;
+    cudaEvent_t ev = run.ev;
     CgState fs;
     MMR_CUDA(cudaMemcpyAsync(&fs, sp, sizeof(CgState), cudaMemcpyDeviceToHost, st));
     float2* xo = (float2*)stage_out(w.sxo, x_user, n * 8);
@@ -473,7 +488,7 @@ static void cg_solve(SenseOp& a, const void* b_user, const void* x0_user, const 
         hist->n = fs.nit + 1;
         hist->status = fs.status;
         // cgne.m:305 sets stopThresh = 0 once the discrepancy rule has fired
-        hist->stop_thresh = h.has_stop ? fs.stop_thresh : stop_thresh_out;
+        hist->stop_thresh = run.has_stop ? fs.stop_thresh : run.stop_thresh_out;
         const int m = std::min(hist->capacity, fs.nit + 1);
         std::vector<double> hh((size_t)4 * cap);
         MMR_CUDA(cudaMemcpy(hh.data(), w.hist.p, hh.size() * sizeof(double), cudaMemcpyDeviceToHost));
@@ -487,7 +502,132 @@ static void cg_solve(SenseOp& a, const void* b_user, const void* x0_user, const 
     MMR_CUDA(cudaEventRecord(ev, st));
     MMR_CUDA(cudaStreamWaitEvent(ust, ev, 0));
     cudaEventDestroy(ev);
+    run.ev = nullptr;
     if (device_error_word(st)) MMR_THROW(MMR_ERR_TIMEOUT, "a bounded device wait ran out during cgne");
+}
+
+static void cg_solve(SenseOp& a, const void* b_user, const void* x0_user, const float* W, const mmr_cgne_opts& o,
+                     void* x_user, mmr_cgne_hist* hist, cudaStream_t ust) {
+    CgRun run = cg_begin(a, b_user, x0_user, W, o, ust);
+    CgWorkspace& w = *static_cast<CgWorkspace*>(a.solver_ws);
+    cudaStream_t st = a.stream;
+    CgState* sp = w.state.as<CgState>();
+    // graphs (re-captured when buffers or options that change kernel arguments differ)
+    const void* key[8] = {a.d_wnorm.p, a.s_grid.p, a.s_grid2.p, w.x.p, w.hist.p, (const void*)(intptr_t)run.has_tik,
+                          (const void*)(intptr_t)run.has_gt, a.nufft ? a.nufft->s_tmp.p : nullptr};
+    const long long keyv[4] = {a.w_bstride, sense_chunk(a), a.nufft && a.nufft->use_bins ? a.nufft->bins.T : 0,
+                               run.cap};
+    bool same = w.g_norm != nullptr;
+    for (int i = 0; i < 8 && same; ++i) same = key[i] == w.key[i];
+    for (int i = 0; i < 4 && same; ++i) same = keyv[i] == w.keyv[i];
+    if (!same) {
+        if (w.g_norm) cudaGraphExecDestroy(w.g_norm);
+        if (w.g_expl) cudaGraphExecDestroy(w.g_expl);
+        w.g_norm = w.g_expl = nullptr;
+        // the eager initial residual has sized every scratch buffer before capture
+        w.g_norm = capture_iter(a, w, false, run.has_tik, run.has_gt, w.k_norm);
+        w.g_expl = capture_iter(a, w, true, run.has_tik, run.has_gt, w.k_expl);
+        for (int i = 0; i < 8; ++i) w.key[i] = key[i];
+        for (int i = 0; i < 4; ++i) w.keyv[i] = keyv[i];
+    }
+    const int poll = run.dynamic ? 4 : run.limit;
+    int it = 0;
+    while (it < run.limit) {
+        const int end = std::min(run.limit, it + poll);
+        for (; it < end; ++it) {
+            const bool ex = it % run.expResN == 0;
+            MMR_CUDA(cudaGraphLaunch(ex ? w.g_expl : w.g_norm, st));
+            add_launches(ex ? w.k_expl : w.k_norm);
+        }
+        int fin = 0;
+        MMR_CUDA(cudaMemcpyAsync(&fin, &sp->finished, sizeof(int), cudaMemcpyDeviceToHost, st));
+        MMR_CUDA(cudaStreamSynchronize(st));
+        if (fin) break;
+    }
+    cg_end(a, run, x_user, hist, ust);
+}
+
+// Many independent solves (slices of different sizes, coil counts and trajectories) advanced
+// together: one CUDA graph holds one iteration of every solve as parallel branches (fork/join
+// on the operators' own streams), so each graph launch moves the whole batch one iteration.
+static void cg_solve_batch(SenseOp* const* ops, int nops, const void* const* b_user, void* const* x_user,
+                           const mmr_cgne_opts& o, mmr_cgne_hist* hists, cudaStream_t ust) {
+    std::vector<CgRun> runs;
+    runs.reserve(nops);
+    for (int i = 0; i < nops; ++i)
+        for (int j = 0; j < i; ++j) MMR_REQUIRE(ops[i] != ops[j], "operators of a batch must be distinct");
+    cudaStream_t origin = nullptr;
+    std::vector<cudaEvent_t> evs;
+    cudaGraphExec_t g[2] = {nullptr, nullptr};
+    auto cleanup = [&] {
+        for (auto e : evs) cudaEventDestroy(e);
+        for (auto& gg : g)
+            if (gg) cudaGraphExecDestroy(gg);
+        if (origin) cudaStreamDestroy(origin);
+        for (int i = 0; i < (int)runs.size(); ++i)
+            if (runs[i].ev) cudaEventDestroy(runs[i].ev);
+    };
+    try {
+        for (int i = 0; i < nops; ++i) runs.push_back(cg_begin(*ops[i], b_user[i], nullptr, nullptr, o, ust));
+        MMR_CUDA(cudaStreamCreateWithFlags(&origin, cudaStreamNonBlocking));
+        evs.resize(nops + 1);
+        for (auto& e : evs) MMR_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        // the origin stream starts after every set-up
+        for (int i = 0; i < nops; ++i) {
+            MMR_CUDA(cudaEventRecord(evs[i], ops[i]->stream));
+            MMR_CUDA(cudaStreamWaitEvent(origin, evs[i], 0));
+        }
+        int kern[2] = {0, 0};
+        for (int v = 0; v < 2; ++v) {
+            g[v] = capture(origin, [&] {
+                MMR_CUDA(cudaEventRecord(evs[nops], origin));
+                for (int i = 0; i < nops; ++i) {
+                    SenseOp& a = *ops[i];
+                    MMR_CUDA(cudaStreamWaitEvent(a.stream, evs[nops], 0));
+                    iter_body(a, *static_cast<CgWorkspace*>(a.solver_ws), v == 1, runs[i].has_tik, runs[i].has_gt,
+                              a.stream);
+                    MMR_CUDA(cudaEventRecord(evs[i], a.stream));
+                    MMR_CUDA(cudaStreamWaitEvent(origin, evs[i], 0));
+                }
+            }, kern[v]);
+        }
+        int limit = 0;
+        bool dynamic = false;
+        for (auto& r : runs) {
+            limit = std::max(limit, r.limit);
+            dynamic = dynamic || r.dynamic;
+        }
+        const int expResN = runs.empty() ? 1 : runs[0].expResN;
+        const int poll = dynamic ? 4 : limit;
+        std::vector<int> fin(nops);
+        int it = 0;
+        while (it < limit) {
+            const int end = std::min(limit, it + poll);
+            for (; it < end; ++it) {
+                const int v = it % expResN == 0 ? 1 : 0;
+                MMR_CUDA(cudaGraphLaunch(g[v], origin));
+                add_launches(kern[v]);
+            }
+            bool all = true;
+            for (int i = 0; i < nops; ++i) {
+                CgState* sp = static_cast<CgWorkspace*>(ops[i]->solver_ws)->state.as<CgState>();
+                MMR_CUDA(cudaMemcpyAsync(&fin[i], &sp->finished, sizeof(int), cudaMemcpyDeviceToHost, origin));
+            }
+            MMR_CUDA(cudaStreamSynchronize(origin));
+            for (int i = 0; i < nops; ++i) all = all && fin[i];
+            if (all) break;
+        }
+        // each operator's stream continues after the last batch graph
+        MMR_CUDA(cudaEventRecord(evs[nops], origin));
+        for (int i = 0; i < nops; ++i) {
+            MMR_CUDA(cudaStreamWaitEvent(ops[i]->stream, evs[nops], 0));
+            cg_end(*ops[i], runs[i], x_user[i], hists ? hists + i : nullptr, ust);
+        }
+    } catch (...) {
+        cleanup();
+        throw;
+    }
+    cleanup();
 }
 
 }  // namespace mmr
@@ -521,5 +661,21 @@ extern "C" int mmr_cgne_solve(mmr_sense* A, const void* b, const void* x0, const
         if (opts) o = *opts;
         else mmr_cgne_default_opts(&o);
         cg_solve(A->a, b, x0, W, o, x_out, hist, as_stream(stream));
+    });
+}
+
+extern "C" int mmr_cgne_solve_batch(mmr_sense* const* A, int32_t n, const void* const* b, void* const* x_out,
+                                    const mmr_cgne_opts* opts, mmr_cgne_hist* hists, void* stream) {
+    return guarded([&] {
+        MMR_REQUIRE(A && b && x_out && n > 0, "NULL argument or empty batch");
+        std::vector<SenseOp*> ops(n);
+        for (int i = 0; i < n; ++i) {
+            MMR_REQUIRE(A[i] && b[i] && x_out[i], "NULL operator, data or output in slot %d", i);
+            ops[i] = &A[i]->a;
+        }
+        mmr_cgne_opts o;
+        if (opts) o = *opts;
+        else mmr_cgne_default_opts(&o);
+        cg_solve_batch(ops.data(), n, b, x_out, o, hists, as_stream(stream));
     });
 }

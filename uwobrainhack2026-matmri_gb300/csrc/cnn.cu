@@ -8,7 +8,8 @@
 //                ReLU mask of the layer input
 //   weight grad  conv3x3_wgrad: per-CTA partial sums over a grid-stride loop of
 //                16 x 16 tiles, then a fixed-order reduction (deterministic)
-//   loss         relative masked L2 per image, FP64 reductions
+//   loss         per image over the interior mask, FP64 reductions: relative L2,
+//                or 1 - cosine^2 between output and target (scale invariant)
 //   optimiser    Adam on the FP32 parameter vector
 // Inference: the same forward, or the tensor-core path for the hidden
 // layers (cnn_mma.cu).
@@ -20,7 +21,7 @@
 namespace mmr {
 
 void cnn_forward_mma(CnnNet& n, int layer, const __nv_bfloat16* in, __nv_bfloat16* out, int nx, int ny, int batch,
-                     cudaStream_t st);
+                     bool relu, cudaStream_t st);
 void cnn_pack_mma(CnnNet& n, cudaStream_t st);
 
 // ------------------------------------------------------------ load / store ----
@@ -37,6 +38,7 @@ struct ConvArgs {
     const void* mask;        // OUT_MASK: activation [B][P][COUT] (ReLU output of the layer input)
     const float2* r;         // OUT_FINAL: network input for the skip path
     const float* skip;       // OUT_FINAL: device scalar
+    int relu;                // 0: identity activations (a linear network)
 };
 
 __device__ __forceinline__ float image_scale(const double* sumsq, int b, long long P, float* inv) {
@@ -132,8 +134,8 @@ __global__ void __launch_bounds__(256, 2) conv3x3_simt(const TIn* __restrict__ i
 #pragma unroll
             for (int co = 0; co < COUT; ++co) {
                 float v = acc[co];
-                if (MODE & OUT_RELU) v = fmaxf(v, 0.f);
-                if (MODE & OUT_MASK) {
+                if ((MODE & OUT_RELU) && a.relu) v = fmaxf(v, 0.f);
+                if ((MODE & OUT_MASK) && a.relu) {
                     if (!(ldf(static_cast<const TMask*>(a.mask) + gp * COUT + co) > 0.f)) v = 0.f;
                 }
                 stf(out + gp * COUT + co, v);
@@ -265,52 +267,65 @@ __global__ void cnn_pack_kernel(const float* __restrict__ W, int cin, int cout, 
     wpkT[(co * 9 + (8 - t)) * cin + ci] = w;
 }
 
-// per image: num[b] = sum m |z - e|^2, den[b] = sum m |e|^2
+// Per image over the interior mask m, LOSS_ACC values: sum |z-e|^2, sum |e|^2, sum |z|^2,
+// re and im of sum conj(z) e.
+constexpr int LOSS_ACC = 5;
+
 __global__ void cnn_loss_reduce_kernel(const float2* __restrict__ z, const float2* __restrict__ e, int X, int Y,
                                        int margin, double* __restrict__ acc) {
     const int b = blockIdx.y;
     const long long P = (long long)X * Y;
-    double sn = 0, sd = 0;
+    double v[LOSS_ACC] = {0, 0, 0, 0, 0};
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < P; i += (long long)gridDim.x * blockDim.x) {
         const int x = (int)(i % X), y = (int)(i / X);
         if (x < margin || x >= X - margin || y < margin || y >= Y - margin) continue;
         const float2 zv = z[(long long)b * P + i], ev = e[(long long)b * P + i];
         const double dx = (double)zv.x - ev.x, dy = (double)zv.y - ev.y;
-        sn += dx * dx + dy * dy;
-        sd += (double)ev.x * ev.x + (double)ev.y * ev.y;
+        v[0] += dx * dx + dy * dy;
+        v[1] += (double)ev.x * ev.x + (double)ev.y * ev.y;
+        v[2] += (double)zv.x * zv.x + (double)zv.y * zv.y;
+        v[3] += (double)zv.x * ev.x + (double)zv.y * ev.y;
+        v[4] += (double)zv.x * ev.y - (double)zv.y * ev.x;
     }
-    for (int o = 16; o; o >>= 1) {
-        sn += __shfl_xor_sync(0xffffffffu, sn, o);
-        sd += __shfl_xor_sync(0xffffffffu, sd, o);
-    }
-    __shared__ double red[2][8];
-    if ((threadIdx.x & 31) == 0) {
-        red[0][threadIdx.x >> 5] = sn;
-        red[1][threadIdx.x >> 5] = sd;
+    __shared__ double red[LOSS_ACC][8];
+#pragma unroll
+    for (int k = 0; k < LOSS_ACC; ++k) {
+        double s = v[k];
+        for (int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if ((threadIdx.x & 31) == 0) red[k][threadIdx.x >> 5] = s;
     }
     __syncthreads();
-    if (threadIdx.x == 0) {
-        double a0 = 0, a1 = 0;
-        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
-            a0 += red[0][w];
-            a1 += red[1][w];
-        }
-        atomicAdd(acc + 2 * b, a0);
-        atomicAdd(acc + 2 * b + 1, a1);
+    if (threadIdx.x < LOSS_ACC) {
+        double t = 0;
+        for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[threadIdx.x][w];
+        atomicAdd(acc + LOSS_ACC * b + threadIdx.x, t);
     }
 }
 
-// gv = s * 2 m (z - e) / den / B  (gradient w.r.t. the last conv output); dskip += sum gv * r / s
+// gv = s * dL/dz (the gradient w.r.t. the last conv output); dskip += sum gv * r / s.
+//   relative L2:  dL/dz = 2 m (z - e) / E / B
+//   cosine:       dL/dz = m (-2 conj(c) e / (Z E) + 2 |c|^2 z / (Z^2 E)) / B,  c = sum conj(z) e
 __global__ void cnn_loss_grad_kernel(const float2* __restrict__ z, const float2* __restrict__ e,
                                      const float2* __restrict__ r, const double* __restrict__ sumsq,
-                                     const double* __restrict__ acc, int X, int Y, int B, int margin,
+                                     const double* __restrict__ acc, int X, int Y, int B, int margin, int cosine,
                                      float2* __restrict__ gv, double* __restrict__ dskip) {
     const int b = blockIdx.y;
     const long long P = (long long)X * Y;
     float inv_s;
     const float s = image_scale(sumsq, b, P, &inv_s);
-    const double den = acc[2 * b + 1] > 0 ? acc[2 * b + 1] : 1.0;
-    const float coef = (float)(2.0 * s / den / B);
+    const double* a = acc + LOSS_ACC * b;
+    const double E = a[1] > 0 ? a[1] : 1.0;
+    // g = ce * e + cz * z with complex ce, real cz
+    double cer = 0, cei = 0, cz = 0;
+    if (!cosine) {
+        cz = 2.0 / E / B;
+        cer = -cz;
+    } else if (a[2] > 0) {
+        const double Z = a[2], c2 = a[3] * a[3] + a[4] * a[4];
+        cer = -2.0 * a[3] / (Z * E) / B;          // -2 conj(c) / (Z E) / B
+        cei = 2.0 * a[4] / (Z * E) / B;
+        cz = 2.0 * c2 / (Z * Z * E) / B;
+    }
     double ds = 0;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < P; i += (long long)gridDim.x * blockDim.x) {
         const int x = (int)(i % X), y = (int)(i / X);
@@ -318,7 +333,8 @@ __global__ void cnn_loss_grad_kernel(const float2* __restrict__ z, const float2*
         float2 g = make_float2(0.f, 0.f);
         if (!(x < margin || x >= X - margin || y < margin || y >= Y - margin)) {
             const float2 zv = z[gp], ev = e[gp];
-            g = make_float2(coef * (zv.x - ev.x), coef * (zv.y - ev.y));
+            g = make_float2((float)(s * (cer * ev.x - cei * ev.y + cz * zv.x)),
+                            (float)(s * (cer * ev.y + cei * ev.x + cz * zv.y)));
         }
         gv[gp] = g;
         const float2 rv = r[gp];
@@ -416,35 +432,36 @@ static void ensure_scratch(CnnNet& n, long long P, int B, bool training, bool fp
     }
     n.z.ensure((size_t)P * B * 8);
     n.sumsq.ensure((size_t)B * 8);
-    n.lossacc.ensure((size_t)B * 16);
+    n.lossacc.ensure((size_t)B * LOSS_ACC * 8);
     n.dskip.ensure(8);
 }
 
 template <class TAct>
-static void forward_simt(CnnNet& n, const float2* r, float2* z, int X, int Y, int B, bool keep, cudaStream_t st) {
+static void forward_simt(CnnNet& n, const float2* r, float2* z, int X, int Y, int B, bool keep, bool relu,
+                         cudaStream_t st) {
     const long long P = (long long)X * Y;
     const size_t per = (size_t)P * B * CNN_HIDDEN;
     TAct* acts = n.act.as<TAct>();
     auto act = [&](int i) { return acts + (keep ? (size_t)i : (size_t)(i & 1)) * per; };   // a_{i+1}
     const float* wpk = n.wpk.as<float>();
-    ConvArgs a{X, Y, n.sumsq.as<double>(), nullptr, r, n.theta.as<float>() + n.nparam - 1};
+    ConvArgs a{X, Y, n.sumsq.as<double>(), nullptr, r, n.theta.as<float>() + n.nparam - 1, relu ? 1 : 0};
     launch_conv<2, CNN_HIDDEN, float2, TAct, TAct, IN_CPLX | OUT_RELU>(r, act(0), wpk + n.woff[0], a, B, st);
     for (int l = 1; l < n.L - 1; ++l)
         launch_conv<CNN_HIDDEN, CNN_HIDDEN, TAct, TAct, TAct, OUT_RELU>(act(l - 1), act(l), wpk + n.woff[l], a, B, st);
     launch_conv<CNN_HIDDEN, 2, TAct, float2, TAct, OUT_FINAL>(act(n.L - 2), z, wpk + n.woff[n.L - 1], a, B, st);
 }
 
-static void forward_tensor(CnnNet& n, const float2* r, float2* z, int X, int Y, int B, cudaStream_t st) {
+static void forward_tensor(CnnNet& n, const float2* r, float2* z, int X, int Y, int B, bool relu, cudaStream_t st) {
     const long long P = (long long)X * Y;
     const size_t per = (size_t)P * B * CNN_HIDDEN;
     __nv_bfloat16* acts = n.act.as<__nv_bfloat16>();
     const float* wpk = n.wpk.as<float>();
-    ConvArgs a{X, Y, n.sumsq.as<double>(), nullptr, r, n.theta.as<float>() + n.nparam - 1};
+    ConvArgs a{X, Y, n.sumsq.as<double>(), nullptr, r, n.theta.as<float>() + n.nparam - 1, relu ? 1 : 0};
     launch_conv<2, CNN_HIDDEN, float2, __nv_bfloat16, __nv_bfloat16, IN_CPLX | OUT_RELU>(r, acts, wpk + n.woff[0], a,
                                                                                          B, st);
     int cur = 0;
     for (int l = 1; l < n.L - 1; ++l) {
-        cnn_forward_mma(n, l, acts + cur * per, acts + (cur ^ 1) * per, X, Y, B, st);
+        cnn_forward_mma(n, l, acts + cur * per, acts + (cur ^ 1) * per, X, Y, B, relu, st);
         cur ^= 1;
     }
     launch_conv<CNN_HIDDEN, 2, __nv_bfloat16, float2, __nv_bfloat16, OUT_FINAL>(acts + cur * per, z,
@@ -470,32 +487,33 @@ void cnn_forward(CnnNet& n, const float2* r, float2* z, int X, int Y, int B, con
     } else {
         compute_sumsq(n, r, P, B, st);
     }
-    if (tc) forward_tensor(n, r, z, X, Y, B, st);
-    else if (fp32) forward_simt<float>(n, r, z, X, Y, B, false, st);
-    else forward_simt<__nv_bfloat16>(n, r, z, X, Y, B, false, st);
+    const bool relu = !(flags & CNN_LINEAR);
+    if (tc) forward_tensor(n, r, z, X, Y, B, relu, st);
+    else if (fp32) forward_simt<float>(n, r, z, X, Y, B, false, relu, st);
+    else forward_simt<__nv_bfloat16>(n, r, z, X, Y, B, false, relu, st);
 }
 
 // Loss, gradient (into n.grad) of a batch; returns the loss on the host.
 template <class TAct>
-static double loss_grad(CnnNet& n, const float2* r, const float2* e, int X, int Y, int B, int margin,
-                        cudaStream_t st) {
+static double loss_grad(CnnNet& n, const float2* r, const float2* e, int X, int Y, int B, int margin, bool cosine,
+                        bool relu, cudaStream_t st) {
     const long long P = (long long)X * Y;
     const size_t per = (size_t)P * B * CNN_HIDDEN;
     ensure_scratch(n, P, B, true, sizeof(TAct) == 4);
     cnn_pack(n, st);
     compute_sumsq(n, r, P, B, st);
     float2* z = n.z.as<float2>();
-    forward_simt<TAct>(n, r, z, X, Y, B, true, st);
+    forward_simt<TAct>(n, r, z, X, Y, B, true, relu, st);
     TAct* acts = n.act.as<TAct>();
     auto act = [&](int i) { return acts + (size_t)i * per; };   // a_{i+1}
-    MMR_CUDA(cudaMemsetAsync(n.lossacc.p, 0, (size_t)B * 16, st));
+    MMR_CUDA(cudaMemsetAsync(n.lossacc.p, 0, (size_t)B * LOSS_ACC * 8, st));
     MMR_CUDA(cudaMemsetAsync(n.dskip.p, 0, 8, st));
     const dim3 rg((unsigned)std::min<long long>(cdiv(P, 256), 64), (unsigned)B);
     cnn_loss_reduce_kernel<<<rg, 256, 0, st>>>(z, e, X, Y, margin, n.lossacc.as<double>());
     check_launch("cnn_loss_reduce");
     float2* gv = n.gv.as<float2>();
     cnn_loss_grad_kernel<<<rg, 256, 0, st>>>(z, e, r, n.sumsq.as<double>(), n.lossacc.as<double>(), X, Y, B, margin,
-                                             gv, n.dskip.as<double>());
+                                             cosine ? 1 : 0, gv, n.dskip.as<double>());
     check_launch("cnn_loss_grad");
     cnn_set_skip_grad_kernel<<<1, 1, 0, st>>>(n.dskip.as<double>(), n.grad.as<float>() + n.nparam - 1);
     check_launch("cnn_skip_grad");
@@ -503,7 +521,7 @@ static double loss_grad(CnnNet& n, const float2* r, const float2* e, int X, int 
     const int Lm = n.L - 1;
     launch_wgrad<CNN_HIDDEN, 2, TAct, false>(act(Lm - 1), reinterpret_cast<const float*>(gv), n, Lm, X, Y, B, st);
     float* gb = n.gbuf.as<float>();
-    ConvArgs a{X, Y, n.sumsq.as<double>(), nullptr, nullptr, nullptr};
+    ConvArgs a{X, Y, n.sumsq.as<double>(), nullptr, nullptr, nullptr, relu ? 1 : 0};
     a.mask = act(Lm - 1);
     launch_conv<2, CNN_HIDDEN, float, float, TAct, OUT_MASK>(reinterpret_cast<const float*>(gv), gb,
                                                              n.wpkT.as<float>() + n.woff[Lm], a, B, st);
@@ -517,11 +535,16 @@ static double loss_grad(CnnNet& n, const float2* r, const float2* e, int X, int 
         cur ^= 1;
     }
     launch_wgrad<2, CNN_HIDDEN, float2, true>(r, gb + (size_t)cur * per, n, 0, X, Y, B, st);
-    std::vector<double> h((size_t)2 * B);
+    std::vector<double> h((size_t)LOSS_ACC * B);
     MMR_CUDA(cudaMemcpyAsync(h.data(), n.lossacc.p, h.size() * 8, cudaMemcpyDeviceToHost, st));
     MMR_CUDA(cudaStreamSynchronize(st));
     double L = 0;
-    for (int b = 0; b < B; ++b) L += h[2 * b] / (h[2 * b + 1] > 0 ? h[2 * b + 1] : 1.0);
+    for (int b = 0; b < B; ++b) {
+        const double* a = h.data() + (size_t)LOSS_ACC * b;
+        const double E = a[1] > 0 ? a[1] : 1.0;
+        if (!cosine) L += a[0] / E;
+        else L += a[2] > 0 ? 1.0 - (a[3] * a[3] + a[4] * a[4]) / (a[2] * E) : 1.0;
+    }
     return L / B;
 }
 
@@ -613,9 +636,12 @@ extern "C" int mmr_cnn_loss_grad(mmr_cnn* net, const void* r, const void* e, int
         const size_t bytes = (size_t)nx * ny * batch * 8;
         const float2* rin = (const float2*)stage_in(n.st_in, r, bytes, st);
         const float2* ein = (const float2*)stage_in(n.st_tgt, e, bytes, st);
-        const double L = (flags & CNN_FP32_ACT)
-                             ? loss_grad<float>(n, rin, ein, (int)nx, (int)ny, (int)batch, margin, st)
-                             : loss_grad<__nv_bfloat16>(n, rin, ein, (int)nx, (int)ny, (int)batch, margin, st);
+        const bool cosine = flags & CNN_LOSS_COS;
+        const bool relu = !(flags & CNN_LINEAR);
+        const double L =
+            (flags & CNN_FP32_ACT)
+                ? loss_grad<float>(n, rin, ein, (int)nx, (int)ny, (int)batch, margin, cosine, relu, st)
+                : loss_grad<__nv_bfloat16>(n, rin, ein, (int)nx, (int)ny, (int)batch, margin, cosine, relu, st);
         if (loss) *loss = L;
         if (grad) MMR_CUDA(cudaMemcpy(grad, n.grad.p, (size_t)n.nparam * 4, cudaMemcpyDeviceToHost));
     });

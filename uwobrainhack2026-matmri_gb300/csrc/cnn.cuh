@@ -36,7 +36,7 @@ struct CnnNet {
     Staged st_in, st_out, st_tgt;
 };
 
-enum CnnFlags { CNN_FP32_ACT = 1, CNN_TENSOR = 2 };
+enum CnnFlags { CNN_FP32_ACT = 1, CNN_TENSOR = 2, CNN_LOSS_COS = 4, CNN_LINEAR = 8 };
 
 // z = net(r) for `batch` complex images of nx x ny on device memory.  `sumsq`
 // (device, per image sum |r|^2) may be supplied by the caller (e.g. from a

@@ -32,7 +32,8 @@ __device__ __forceinline__ void mma_bf16(float (&c)[4], uint32_t a0, uint32_t a1
 
 __global__ void __launch_bounds__(256) conv3x3_mma_kernel(const __nv_bfloat16* __restrict__ in,
                                                           __nv_bfloat16* __restrict__ out,
-                                                          const __nv_bfloat16* __restrict__ wmma, int X, int Y) {
+                                                          const __nv_bfloat16* __restrict__ wmma, int X, int Y,
+                                                          int relu) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __nv_bfloat16* s_in = reinterpret_cast<__nv_bfloat16*>(smem_raw);
     __nv_bfloat16* s_w = s_in + MH * MH * PIX_STRIDE;       // [2][32][KSTRIDE]
@@ -93,7 +94,8 @@ __global__ void __launch_bounds__(256) conv3x3_mma_kernel(const __nv_bfloat16* _
             }
         }
     }
-    // epilogue: ReLU, BF16, NHWC
+    // epilogue: ReLU (unless the network is linear), BF16, NHWC
+    auto act = [relu](float v) { return relu ? fmaxf(v, 0.f) : v; };
 #pragma unroll
     for (int m = 0; m < 2; ++m) {
         const int y = y0 + warp * 2 + m;
@@ -105,8 +107,7 @@ __global__ void __launch_bounds__(256) conv3x3_mma_kernel(const __nv_bfloat16* _
             __nv_bfloat16* o = out + ((long long)b * P + (long long)y * X + x) * CNN_HIDDEN;
 #pragma unroll
             for (int n = 0; n < 4; ++n) {
-                const __nv_bfloat162 v = __floats2bfloat162_rn(fmaxf(acc[m][n][2 * hh], 0.f),
-                                                               fmaxf(acc[m][n][2 * hh + 1], 0.f));
+                const __nv_bfloat162 v = __floats2bfloat162_rn(act(acc[m][n][2 * hh]), act(acc[m][n][2 * hh + 1]));
                 *reinterpret_cast<__nv_bfloat162*>(o + n * 8 + 2 * tig) = v;
             }
         }
@@ -140,7 +141,7 @@ void cnn_pack_mma(CnnNet& n, cudaStream_t st) {
 }
 
 void cnn_forward_mma(CnnNet& n, int layer, const __nv_bfloat16* in, __nv_bfloat16* out, int nx, int ny, int batch,
-                     cudaStream_t st) {
+                     bool relu, cudaStream_t st) {
     static bool attr = false;
     if (!attr) {
         MMR_CUDA(cudaFuncSetAttribute(conv3x3_mma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)MMA_SMEM));
@@ -149,7 +150,7 @@ void cnn_forward_mma(CnnNet& n, int layer, const __nv_bfloat16* in, __nv_bfloat1
     const size_t per = (size_t)2 * CNN_HIDDEN * KSTRIDE;
     dim3 grid((unsigned)cdiv(nx, MT), (unsigned)cdiv(ny, MT), (unsigned)batch);
     conv3x3_mma_kernel<<<grid, 256, MMA_SMEM, st>>>(in, out, n.wmma.as<__nv_bfloat16>() + (size_t)(layer - 1) * per,
-                                                   nx, ny);
+                                                   nx, ny, relu ? 1 : 0);
     check_launch("conv3x3_mma");
 }
 

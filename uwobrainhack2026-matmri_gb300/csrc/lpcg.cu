@@ -450,7 +450,7 @@ extern "C" int mmr_lpcg_default_opts(mmr_lpcg_opts* o) {
         memset(o, 0, sizeof(*o));
         o->nit_max = 100;
         o->tol = 0.0;
-        o->stall_window = 5;
+        o->stall_window = 10;
         o->flags = 2;   // tensor-core network forward
         o->poll = 8;
     });

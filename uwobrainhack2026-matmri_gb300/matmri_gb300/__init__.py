@@ -9,8 +9,8 @@ package raises on import of an operator when the library is missing.
 from ._lib import MatmriError, load as load_library
 from .ops import nufftOp, rcvrOp, sampHighOrder
 from .sense import mrSampFunc, mrSampOp
-from .solvers import bfista, cgne, dwtND, powermethod
+from .solvers import bfista, cgne, cgne_batch, dwtND, powermethod
 from .learned import PrecondNet, lpcg
 
-__all__ = ["nufftOp", "rcvrOp", "sampHighOrder", "mrSampFunc", "mrSampOp", "cgne", "powermethod", "bfista",
-           "dwtND", "PrecondNet", "lpcg", "MatmriError", "load_library"]
+__all__ = ["nufftOp", "rcvrOp", "sampHighOrder", "mrSampFunc", "mrSampOp", "cgne", "cgne_batch", "powermethod",
+           "bfista", "dwtND", "PrecondNet", "lpcg", "MatmriError", "load_library"]

@@ -89,6 +89,8 @@ class LpcgHist(C.Structure):
 
 CNN_FP32_ACT = 1
 CNN_TENSOR = 2
+CNN_LOSS_COS = 4
+CNN_LINEAR = 8
 
 # name -> (restype, argtypes)
 SIGNATURES = {
@@ -120,6 +122,8 @@ SIGNATURES = {
     "mmr_cgne_default_opts": (C.c_int, [C.POINTER(CgneOpts)]),
     "mmr_cgne_solve": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.POINTER(C.c_float), C.POINTER(CgneOpts),
                                  C.c_void_p, C.POINTER(CgneHist), C.c_void_p]),
+    "mmr_cgne_solve_batch": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_void_p),
+                                       C.POINTER(C.c_void_p), C.POINTER(CgneOpts), C.POINTER(CgneHist), C.c_void_p]),
     "mmr_powermethod": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_double, C.POINTER(C.c_double),
                                   C.POINTER(C.c_double), C.c_void_p]),
     "mmr_dwt_haar": (C.c_int, [C.c_int32, C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.c_int, C.c_void_p,

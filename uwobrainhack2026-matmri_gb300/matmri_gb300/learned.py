@@ -36,15 +36,22 @@ def init_params(seed: int, channels=CHANNELS) -> np.ndarray:
 
 
 class PrecondNet:
-    """z = net(r) on complex images; parameters FP32 (``theta``), activations BF16."""
+    """z = net(r) on complex images; parameters FP32 (``theta``), activations BF16.
 
-    def __init__(self, params=None, seed: int = 0, channels=CHANNELS):
+    ``linear=True`` (the default) uses identity activations: the network is then a fixed linear
+    operator, which keeps flexible CG as effective as preconditioned CG.  With ReLU activations the
+    preconditioner changes with every residual and the solve stalls far above the target accuracy.
+    """
+
+    def __init__(self, params=None, seed: int = 0, channels=CHANNELS, linear: bool = True):
         lib = _lib.load()
         ch = (C.c_int32 * len(channels))(*channels)
         h = C.c_void_p()
         _lib.check(lib.mmr_cnn_create(len(channels) - 1, ch, C.byref(h)))
         self._h = h
         self.channels = tuple(channels)
+        self.linear = bool(linear)
+        self.base_flags = _lib.CNN_LINEAR if self.linear else 0
         n = C.c_int64()
         _lib.check(lib.mmr_cnn_num_params(h, C.byref(n)))
         self.n_params = int(n.value)
@@ -65,19 +72,22 @@ class PrecondNet:
         _lib.check(_lib.load().mmr_cnn_get_params(self._h, t.ctypes.data))
         return t
 
-    def save(self, path):
-        np.save(path, self.get_params())
+    def save(self, path, **meta):
+        np.savez(path, theta=self.get_params(), channels=np.array(self.channels), linear=self.linear,
+                 **{k: np.asarray(v) for k, v in meta.items()})
 
     @classmethod
     def load(cls, path):
-        return cls(params=np.load(path))
+        f = np.load(path)
+        return cls(params=f["theta"], channels=tuple(int(c) for c in f["channels"]), linear=bool(f["linear"]))
 
     def forward(self, r, flags: int = _lib.CNN_TENSOR):
         """z = net(r) for r [nx, ny] or [nx, ny, batch]."""
         b = as_c64(r)
         shp = tuple(b.shape) + (1,) * (3 - len(b.shape))
         out, optr = alloc_like(b, b.shape)
-        _lib.check(_lib.load().mmr_cnn_forward(self._h, b.ptr, optr, shp[0], shp[1], shp[2], flags, stream_of(b)))
+        _lib.check(_lib.load().mmr_cnn_forward(self._h, b.ptr, optr, shp[0], shp[1], shp[2],
+                                               flags | self.base_flags, stream_of(b)))
         return finish(out, b)
 
     __call__ = forward
@@ -90,8 +100,9 @@ class PrecondNet:
         shp = tuple(rb.shape) + (1,) * (3 - len(rb.shape))
         L = C.c_double()
         g = np.empty(self.n_params, dtype=np.float32) if want_grad else None
-        _lib.check(_lib.load().mmr_cnn_loss_grad(self._h, rb.ptr, eb.ptr, shp[0], shp[1], shp[2], margin, flags,
-                                                 C.byref(L), g.ctypes.data if want_grad else None, stream_of(rb)))
+        _lib.check(_lib.load().mmr_cnn_loss_grad(self._h, rb.ptr, eb.ptr, shp[0], shp[1], shp[2], margin,
+                                                 flags | self.base_flags, C.byref(L),
+                                                 g.ctypes.data if want_grad else None, stream_of(rb)))
         return L.value, g
 
     def adam_step(self, lr: float, stream=None):
@@ -105,7 +116,7 @@ class PrecondNet:
 
 
 def lpcg(A, y, net: PrecondNet | None = None, x0=None, NitMax: int = 100, tol: float = 0.0, lam: float = 0.0,
-         tik_diag=None, gtruth=None, stall_window: int = 5, flags: int = _lib.CNN_TENSOR, poll: int = 8):
+         tik_diag=None, gtruth=None, stall_window: int = 10, flags: int = _lib.CNN_TENSOR, poll: int = 8):
     """x, res_sq, err_sq, info = lpcg(A, y, net, ...): learned-preconditioned CG-SENSE.
 
     Solves (A'A + lam + diag(tik_diag)) x = A'y like ``cgne(A, y, x0, NitMax, opt, gam, R)`` with
@@ -119,7 +130,7 @@ def lpcg(A, y, net: PrecondNet | None = None, x0=None, NitMax: int = 100, tol: f
     o.tol = float(tol)
     o.lam = float(lam)
     o.stall_window = int(stall_window)
-    o.flags = int(flags)
+    o.flags = int(flags) | (net.base_flags if net is not None else 0)
     o.poll = int(poll)
     keep = []
     if tik_diag is not None:
@@ -179,28 +190,35 @@ def cg_iterates(normal, b, lam: float, nit: int, keep_at):
 
 
 def train(net: PrecondNet, R, E, steps: int = 3000, batch: int = 64, crop: int = 64, margin: int = 6,
-          lr: float = 1e-3, lr_min: float = 1e-5, seed: int = 0, log_every: int = 0):
+          lr: float = 1e-3, lr_min: float = 1e-5, seed: int = 0, log_every: int = 0,
+          loss_flags: int = _lib.CNN_LOSS_COS):
     """Adam on random crops of the pairs R[i] -> E[i] (torch complex64 [n, nx, ny] on the device,
-    row i the i-th image in (x, y) order); cosine learning-rate decay.  Returns the loss history."""
+    row i the i-th image in (x, y) order); cosine learning-rate decay.  The default loss is the
+    scale-invariant one: flexible CG's line search sets the scale of every direction, so only the
+    direction of net(r) relative to the error matters.  Returns the loss history."""
     import torch
     g = torch.Generator(device=R.device)
     g.manual_seed(seed)
     n, nx, ny = R.shape
     losses = []
+    # crops may reach `margin` pixels past the image (zero there, as the network's own zero
+    # padding sees it), so the pixels at the image border are inside some crop's loss mask
+    ar = torch.arange(crop, device=R.device)
     for s in range(steps):
         i = torch.randint(0, n, (batch,), generator=g, device=R.device)
-        ox = torch.randint(0, nx - crop + 1, (batch,), generator=g, device=R.device)
-        oy = torch.randint(0, ny - crop + 1, (batch,), generator=g, device=R.device)
-        ar = torch.arange(crop, device=R.device)
+        ox = torch.randint(-margin, nx - crop + margin + 1, (batch,), generator=g, device=R.device)
+        oy = torch.randint(-margin, ny - crop + margin + 1, (batch,), generator=g, device=R.device)
         ix = (ox[:, None] + ar[None, :])[:, :, None].expand(batch, crop, crop)
         iy = (oy[:, None] + ar[None, :])[:, None, :].expand(batch, crop, crop)
+        inside = (ix >= 0) & (ix < nx) & (iy >= 0) & (iy < ny)
         ii = i[:, None, None].expand(batch, crop, crop)
-        rc = R[ii, ix, iy]            # [batch, crop(x), crop(y)]
-        ec = E[ii, ix, iy]
+        cx, cy = ix.clamp(0, nx - 1), iy.clamp(0, ny - 1)
+        rc = torch.where(inside, R[ii, cx, cy], 0)       # [batch, crop(x), crop(y)]
+        ec = torch.where(inside, E[ii, cx, cy], 0)
         # column-major [x, y, batch] views of contiguous [batch, y, x] storage
         rb = rc.permute(0, 2, 1).contiguous().permute(2, 1, 0)
         eb = ec.permute(0, 2, 1).contiguous().permute(2, 1, 0)
-        L, _ = net.loss_grad(rb, eb, margin, 0, want_grad=False)
+        L, _ = net.loss_grad(rb, eb, margin, loss_flags, want_grad=False)
         cur = lr_min + 0.5 * (lr - lr_min) * (1 + math.cos(math.pi * s / max(1, steps - 1)))
         net.adam_step(cur, torch.cuda.current_stream(R.device).cuda_stream)
         losses.append(L)

@@ -48,13 +48,10 @@ def _tik_diag(op, gam, R):
     return np.ascontiguousarray(acc.astype(np.float32))
 
 
-def cgne(A, b, x0=None, NitMax=None, opt=None, gam=None, R=None, W=None):
-    """[x, resSqAll, mseAll, xnormAll, xdiffAll, stopThresh, status] = cgne(A, b, x0, NitMax, opt, gam, R, W)."""
-    op = resolve_operator(A)
-    lib = _lib.load()
-    o = dict(opt or {})
+def _scalar_opts(o, NitMax):
+    """cgne's scalar options (cgne.m:21-89) in the C struct; absent fields keep the defaults."""
     co = _lib.CgneOpts()
-    _lib.check(lib.mmr_cgne_default_opts(C.byref(co)))
+    _lib.check(_lib.load().mmr_cgne_default_opts(C.byref(co)))
     co.nit_max = 1000 if NitMax is None else int(NitMax)
     if "resThresh" in o: co.res_thresh = _d(o["resThresh"])
     if "resChangeThresh" in o: co.res_change_thresh = _d(o["resChangeThresh"])
@@ -66,6 +63,15 @@ def cgne(A, b, x0=None, NitMax=None, opt=None, gam=None, R=None, W=None):
     if "resIncThresh" in o: co.res_inc_thresh = float(o["resIncThresh"])
     if "stopOnXdifInc" in o: co.stop_on_xdif_inc = int(o["stopOnXdifInc"])
     if "noiseVar" in o: co.noise_var = _d(o["noiseVar"])
+    return co
+
+
+def cgne(A, b, x0=None, NitMax=None, opt=None, gam=None, R=None, W=None):
+    """[x, resSqAll, mseAll, xnormAll, xdiffAll, stopThresh, status] = cgne(A, b, x0, NitMax, opt, gam, R, W)."""
+    op = resolve_operator(A)
+    lib = _lib.load()
+    o = dict(opt or {})
+    co = _scalar_opts(o, NitMax)
     keep = []
     if o.get("noise") is not None:
         nb = as_c64(o["noise"])
@@ -116,6 +122,41 @@ def cgne(A, b, x0=None, NitMax=None, opt=None, gam=None, R=None, W=None):
         x = x.permute(*range(x.dim() - 1, -1, -1)).reshape(-1) if is_torch(x) else np.reshape(x, -1, order="F")
     st = None if math.isnan(h.stop_thresh) else h.stop_thresh
     return x, hist_arr[0, :n].copy(), hist_arr[1, :n].copy(), hist_arr[2, :n].copy(), hist_arr[3, :n].copy(), st, h.status
+
+
+def cgne_batch(As, bs, NitMax=None, opt=None):
+    """xs, infos = cgne_batch([A_1..A_n], [b_1..b_n], NitMax, opt): n independent cgne solves (the
+    reference loops cgne over slices) advanced together, one CUDA graph launch per iteration for the
+    whole batch.  Scalar options as cgne's; x0 = A_i'b_i; infos[i] holds resSqAll, xnormAll, xdiffAll,
+    status and nit of solve i."""
+    ops = [resolve_operator(A) for A in As]
+    n = len(ops)
+    if n == 0 or len(bs) != n:
+        raise ValueError("cgne_batch needs one data array per operator")
+    if len({id(op) for op in ops}) != n:
+        raise ValueError("the operators of a batch must be distinct")
+    lib = _lib.load()
+    co = _scalar_opts(dict(opt or {}), NitMax)
+    bufs = [as_c64(b) for b in bs]
+    outs = [alloc_like(bb, op.imN) for bb, op in zip(bufs, ops)]
+    cap = co.nit_max + max(co.nse_extra_it, 0) + 1
+    harr = np.zeros((n, 4, cap), dtype=np.float64)
+    hs = (_lib.CgneHist * n)()
+    for i in range(n):
+        hs[i].res_sq = _lib.dptr(harr[i, 0])
+        hs[i].mse = _lib.dptr(harr[i, 1])
+        hs[i].xnorm = _lib.dptr(harr[i, 2])
+        hs[i].xdiff = _lib.dptr(harr[i, 3])
+        hs[i].capacity = cap
+    handles = (C.c_void_p * n)(*[op.handle for op in ops])
+    bptr = (C.c_void_p * n)(*[bb.ptr for bb in bufs])
+    xptr = (C.c_void_p * n)(*[p for _, p in outs])
+    _lib.check(lib.mmr_cgne_solve_batch(handles, n, bptr, xptr, C.byref(co), hs, stream_of(bufs[0])))
+    xs = [finish(o_, bb) for (o_, _), bb in zip(outs, bufs)]
+    infos = [{"resSqAll": harr[i, 0, :hs[i].n].copy(), "xnormAll": harr[i, 2, :hs[i].n].copy(),
+              "xdiffAll": harr[i, 3, :hs[i].n].copy(), "status": hs[i].status, "nit": hs[i].nit}
+             for i in range(n)]
+    return xs, infos
 
 
 def powermethod(A, x0, NitMax=None, doAtA=None, xdiffThresh=None):

@@ -95,6 +95,59 @@ def coil_maps(N: int, C: int, seed: int = 0, randomize: bool = False) -> np.ndar
     return maps / rss
 
 
+def _grid_torch(N, scale, device):
+    import torch
+    c = (torch.arange(N, dtype=torch.float64, device=device) - N / 2) / scale
+    X, Y = torch.meshgrid(c, c, indexing="ij")
+    return X, Y
+
+
+def ellipse_phantom_torch(N: int, n_ellipses: int = 10, seed: int = 0, complex_phase: bool = False,
+                          device="cuda"):
+    """``ellipse_phantom`` evaluated with torch on `device` (same draws; complex64 [N, N], column-major)."""
+    import torch
+    g = rng(seed)
+    X, Y = _grid_torch(N, N / 2, device)
+    img = torch.zeros((N, N), dtype=torch.float64, device=device)
+    for _ in range(n_ellipses):
+        cx, cy = g.uniform(-0.6, 0.6, 2)
+        a, b = g.uniform(0.05, 0.45, 2)
+        th = g.uniform(0, math.pi)
+        val = g.uniform(0, 1)
+        xr = (X - cx) * math.cos(th) + (Y - cy) * math.sin(th)
+        yr = -(X - cx) * math.sin(th) + (Y - cy) * math.cos(th)
+        img += val * ((xr / a) ** 2 + (yr / b) ** 2 <= 1.0).to(torch.float64)
+    out = img.to(torch.complex128)
+    if complex_phase:
+        co = g.uniform(-1, 1, 6)
+        ph = co[0] + co[1] * X + co[2] * Y + co[3] * X * Y + co[4] * X ** 2 + co[5] * Y ** 2
+        ph = ph / max(float(ph.abs().max()), 1e-12) * (math.pi / 2)
+        out = out * torch.exp(1j * ph)
+    return out.to(torch.complex64).T.contiguous().T
+
+
+def coil_maps_torch(N: int, C: int, seed: int = 0, randomize: bool = False, device="cuda"):
+    """``coil_maps`` evaluated with torch on `device` (same draws; complex64 [N, N, C], column-major)."""
+    import torch
+    g = rng(seed)
+    fov = 1.0
+    X, Y = _grid_torch(N, N / fov, device)
+    radius, sigma = 0.6 * fov / 2, 0.35 * fov
+    maps = torch.empty((C, N, N), dtype=torch.complex128, device=device)
+    for ci in range(C):
+        rr = radius * (g.uniform(0.8, 1.2) if randomize else 1.0)
+        ss = sigma * (g.uniform(0.8, 1.2) if randomize else 1.0)
+        ang = 2 * math.pi * ci / C
+        cx, cy = rr * math.cos(ang), rr * math.sin(ang)
+        mag = torch.exp(-((X - cx) ** 2 + (Y - cy) ** 2) / (2 * ss ** 2))
+        a, b = g.uniform(-math.pi, math.pi, 2) / fov
+        c0 = g.uniform(-math.pi, math.pi)
+        maps[ci] = mag * torch.exp(1j * (a * X + b * Y + c0))
+    maps = maps / torch.sqrt((maps.abs() ** 2).sum(dim=0, keepdim=True))
+    # [C, N1, N2] -> column-major [N1, N2, C]
+    return maps.to(torch.complex64).permute(0, 2, 1).contiguous().permute(2, 1, 0)
+
+
 def add_noise(y: np.ndarray, snr: float, seed: int) -> np.ndarray:
     g = rng(seed)
     sig = math.sqrt(np.mean(np.abs(y) ** 2)) / snr

@@ -181,3 +181,30 @@ def test_converged_image_matches_fp64(mm):
     xg, _, _, _ = lpcg(A, y.astype(np.complex64), None, NitMax=300, lam=lam)
     xg, _, _, _ = lpcg(A, y.astype(np.complex64), None, x0=xg, NitMax=100, lam=lam)
     assert rel(xg, x64) < 1e-4
+
+
+def test_trained_network_gain(mm):
+    """What the committed, trained network gains over plain CG on a held-out 256 x 256, 32-coil,
+    R = 4, SNR-30 case: iterations to NRMSE 1e-3 against the converged image."""
+    import os
+    import torch
+    from matmri_gb300 import synth
+    from matmri_gb300.learned import PrecondNet, iterations_to, lpcg
+    from matmri_gb300 import train_precond as tp
+    assert os.path.exists(tp.WEIGHTS)
+    meta = np.load(tp.WEIGHTS)
+    lam = float(meta["lam"])
+    net = PrecondNet.load(tp.WEIGHTS)
+    c = synth.sense_case(256, 32, 4, 4096, 4.0, seed=5001, randomize_coils=True)
+    A = mm.mrSampOp(mm.nufftOp([256, 256], c["kloc"], None, 1, 2.0, 4), mm.rcvrOp(c["maps"], 0))
+    y = synth.add_noise(np.asarray(A(c["img"].astype(np.complex64), "notransp"), dtype=np.complex128), 30.0, 5008)
+    yd = torch.from_numpy(np.ascontiguousarray(y.astype(np.complex64).T)).cuda().T
+    xs, _, _, _ = lpcg(A, yd, None, NitMax=300, lam=lam)
+    xs, _, _, _ = lpcg(A, yd, None, x0=xs, NitMax=100, lam=lam)
+    gn = float(torch.linalg.norm(xs))
+    _, _, e_plain, _ = lpcg(A, yd, None, NitMax=120, lam=lam, gtruth=xs)
+    _, _, e_learn, info = lpcg(A, yd, net, NitMax=120, lam=lam, gtruth=xs)
+    k_plain, k_learn = iterations_to(e_plain, gn), iterations_to(e_learn, gn)
+    assert k_plain is not None and k_learn is not None
+    assert info["fell_back_at"] == -1
+    assert k_learn <= 0.7 * k_plain, (k_learn, k_plain)

@@ -308,7 +308,8 @@ MMR_API int mmr_bfista_solve(mmr_sense* A, const void* b, const int32_t* levels,
 typedef struct mmr_cnn mmr_cnn;
 
 #define MMR_CNN_FP32_ACT 1   /* keep activations in FP32 (default BF16)       */
-#define MMR_CNN_TENSOR   2   /* tensor-core forward of the hidden layers      */
+#define MMR_CNN_TENSOR   2   /* forward on the tensor-core path (mma.sync, FP16
+                                activations, FP32 accumulation)               */
 #define MMR_CNN_LOSS_COS 4   /* loss_grad: 1 - |<z,e>|^2/(|z|^2 |e|^2) instead of
                                 the relative L2 (invariant to a complex scale)  */
 #define MMR_CNN_LINEAR   8   /* identity activations: the network is a fixed
@@ -347,6 +348,8 @@ typedef struct mmr_lpcg_opts {
     int32_t       stall_window;  /* fallback window (default 10; 0 = never)       */
     int32_t       flags;         /* MMR_CNN_* network flags (default TENSOR)      */
     int32_t       poll;          /* host checks the device flags every poll its (8) */
+    int32_t       fcg_m;         /* directions the new one is made H-conjugate to
+                                    (1..8, default 4; plain CG uses 1)          */
 } mmr_lpcg_opts;
 
 typedef struct mmr_lpcg_hist {

@@ -160,11 +160,11 @@ def adam_step(theta, grad, m, v, t, lr, b1=0.9, b2=0.999, eps=1e-8):
     return theta - lr * mh / (np.sqrt(vh) + eps), m, v
 
 
-def fcg_ref(normal, b, precond, nit, lam=0.0, x0=None, gtruth=None):
-    """Flexible PCG on (H + lam I) x = b with H = normal(.) Hermitian and z = precond(r).
+def fcg_ref(normal, b, precond, nit, lam=0.0, x0=None, gtruth=None, m=1):
+    """Flexible PCG (FCG(m)) on (H + lam I) x = b with H = normal(.) Hermitian and z = precond(r).
 
       alpha = (p' r) / (p' q),  q = (H + lam) p      exact line search along p
-      beta  = -(q' z_new) / (p' q)                   z_new conjugated against p
+      p_new = z - sum_j (q_j' z) / (p_j' q_j) p_j    z conjugated against the last m directions
     With precond = identity this is CG.  Returns (x, res_sq history, nrmse history).
     """
     b = np.asarray(b, dtype=np.complex128)
@@ -177,15 +177,18 @@ def fcg_ref(normal, b, precond, nit, lam=0.0, x0=None, gtruth=None):
     gn = None if gtruth is None else np.linalg.norm(gtruth)
     if gtruth is not None:
         err.append(float(np.linalg.norm(x - gtruth) / gn))
+    hist = []
     for _ in range(nit):
         q = Hx(p)
         pq = np.vdot(p, q)
         alpha = np.vdot(p, r) / pq
         x = x + alpha * p
         r = r - alpha * q
+        hist = (hist + [(p, q, pq)])[-m:]
         z = precond(r)
-        beta = -np.vdot(q, z) / pq
-        p = z + beta * p
+        p = z.copy()
+        for pj, qj, pqj in hist:
+            p = p - (np.vdot(qj, z) / pqj) * pj
         res.append(float(np.vdot(r, r).real))
         if gtruth is not None:
             err.append(float(np.linalg.norm(x - gtruth) / gn))

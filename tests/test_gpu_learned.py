@@ -127,8 +127,9 @@ def test_lpcg_plain_is_cg(mm):
     assert info["nit"] == 12 and info["fell_back_at"] == -1
 
 
+@pytest.mark.parametrize("m", [1, 3, 8])
 @pytest.mark.parametrize("linear", [False, True])
-def test_lpcg_learned_matches_oracle(mm, linear):
+def test_lpcg_learned_matches_oracle(mm, linear, m):
     from matmri_gb300.learned import PrecondNet, lpcg
     from matmri_gb300 import _lib
     A, y, b, normal = _sense(mm, seed=1)
@@ -137,8 +138,8 @@ def test_lpcg_learned_matches_oracle(mm, linear):
     net = PrecondNet(theta, linear=linear)
     pre = lambda r: cnn_ref.forward(theta.astype(np.float64), r[None], linear=linear)[0]
     lam = 0.5
-    x, res, _, info = lpcg(A, y, net, NitMax=6, lam=lam, flags=_lib.CNN_FP32_ACT, stall_window=0)
-    xr, res_r, _ = cnn_ref.fcg_ref(normal, b, pre, 6, lam=lam)
+    x, res, _, info = lpcg(A, y, net, NitMax=10, lam=lam, flags=_lib.CNN_FP32_ACT, stall_window=0, fcg_m=m)
+    xr, res_r, _ = cnn_ref.fcg_ref(normal, b, pre, 10, lam=lam, m=m)
     assert rel(x, xr) < 1e-3
     np.testing.assert_allclose(res, res_r, rtol=1e-2)
 

@@ -11,8 +11,8 @@
 //   loss         per image over the interior mask, FP64 reductions: relative L2,
 //                or 1 - cosine^2 between output and target (scale invariant)
 //   optimiser    Adam on the FP32 parameter vector
-// Inference: the same forward, or the tensor-core path for the hidden
-// layers (cnn_mma.cu).
+// Inference: the same forward, or the tensor-core path (cnn_mma.cu, FP16
+// activations).
 #include <algorithm>
 #include <cmath>
 
@@ -20,8 +20,8 @@
 
 namespace mmr {
 
-void cnn_forward_mma(CnnNet& n, int layer, const __nv_bfloat16* in, __nv_bfloat16* out, int nx, int ny, int batch,
-                     bool relu, cudaStream_t st);
+void cnn_forward_tensor(CnnNet& n, const float2* r, float2* z, int nx, int ny, int batch, bool relu,
+                        cudaStream_t st);
 void cnn_pack_mma(CnnNet& n, cudaStream_t st);
 
 // ------------------------------------------------------------ load / store ----
@@ -451,23 +451,6 @@ static void forward_simt(CnnNet& n, const float2* r, float2* z, int X, int Y, in
     launch_conv<CNN_HIDDEN, 2, TAct, float2, TAct, OUT_FINAL>(act(n.L - 2), z, wpk + n.woff[n.L - 1], a, B, st);
 }
 
-static void forward_tensor(CnnNet& n, const float2* r, float2* z, int X, int Y, int B, bool relu, cudaStream_t st) {
-    const long long P = (long long)X * Y;
-    const size_t per = (size_t)P * B * CNN_HIDDEN;
-    __nv_bfloat16* acts = n.act.as<__nv_bfloat16>();
-    const float* wpk = n.wpk.as<float>();
-    ConvArgs a{X, Y, n.sumsq.as<double>(), nullptr, r, n.theta.as<float>() + n.nparam - 1, relu ? 1 : 0};
-    launch_conv<2, CNN_HIDDEN, float2, __nv_bfloat16, __nv_bfloat16, IN_CPLX | OUT_RELU>(r, acts, wpk + n.woff[0], a,
-                                                                                         B, st);
-    int cur = 0;
-    for (int l = 1; l < n.L - 1; ++l) {
-        cnn_forward_mma(n, l, acts + cur * per, acts + (cur ^ 1) * per, X, Y, B, relu, st);
-        cur ^= 1;
-    }
-    launch_conv<CNN_HIDDEN, 2, __nv_bfloat16, float2, __nv_bfloat16, OUT_FINAL>(acts + cur * per, z,
-                                                                                wpk + n.woff[n.L - 1], a, B, st);
-}
-
 static void compute_sumsq(CnnNet& n, const float2* r, long long P, int B, cudaStream_t st) {
     MMR_CUDA(cudaMemsetAsync(n.sumsq.p, 0, (size_t)B * 8, st));
     cnn_sumsq_kernel<<<dim3((unsigned)std::min<long long>(cdiv(P, 256), 64), (unsigned)B), 256, 0, st>>>(
@@ -488,7 +471,7 @@ void cnn_forward(CnnNet& n, const float2* r, float2* z, int X, int Y, int B, con
         compute_sumsq(n, r, P, B, st);
     }
     const bool relu = !(flags & CNN_LINEAR);
-    if (tc) forward_tensor(n, r, z, X, Y, B, relu, st);
+    if (tc) cnn_forward_tensor(n, r, z, X, Y, B, relu, st);
     else if (fp32) forward_simt<float>(n, r, z, X, Y, B, false, relu, st);
     else forward_simt<__nv_bfloat16>(n, r, z, X, Y, B, false, relu, st);
 }

@@ -1,5 +1,6 @@
 // Learned preconditioner network: a bias-free 3x3 CNN on complex images
-// (2 real channels), hidden width 32, ReLU between layers, global skip.
+// (2 real channels), hidden width 32, ReLU (or identity: CNN_LINEAR) between
+// layers, global skip.
 //
 //   s  = sqrt(mean |r|^2);  a0 = r / s  (complex = channels 0, 1)
 //   a_{l+1} = relu(conv3x3(a_l, W_l))      l < L-1
@@ -8,8 +9,9 @@
 // Activations are NHWC (channel fastest) over an image whose first index x
 // is the fastest (the column-major MATLAB layout): a complex image is then
 // exactly the 2-channel activation.  Weights are FP32 (theta layout
-// [co][ci][ky][kx] per layer, then skip); hidden activations are stored as
-// BF16 unless the caller asks for FP32.
+// [co][ci][ky][kx] per layer, then skip).  Hidden activations: BF16 in the
+// SIMT path (training) unless the caller asks for FP32; FP16 in the
+// tensor-core inference path (CNN_TENSOR).
 #pragma once
 
 #include <cuda_bf16.h>

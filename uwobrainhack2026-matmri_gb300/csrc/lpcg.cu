@@ -3,12 +3,16 @@
 //     b = A'W y                (cgne.m:136-140)
 // with the preconditioner z = net(r) (cnn.cuh) or z = r (plain CG):
 //     q = H p;  alpha = (p'r)/(p'q);  x += alpha p;  r -= alpha q
-//     z = net(r);  beta = -(q'z)/(p'q);  p = z + beta p
-// alpha is the exact line minimiser of the H-norm error along p, so every
-// step lowers it whatever the network returns; beta makes p H-conjugate to
-// the previous direction.  r is updated with exact H products, so it tracks
-// the true residual b - Hx up to rounding.  The network's first application
-// (to r0 = b when x0 = 0) is the warm start.
+//     z = net(r);  p = z - sum_j (q_j'z)/(p_j'q_j) p_j
+// over the m most recent directions p_j (FCG(m); a ring of (p_j, q_j) in
+// HBM).  alpha is the exact line minimiser of the H-norm error along p, so
+// every step lowers it whatever the network returns; the sum makes p
+// H-conjugate to the last m directions, which keeps the method close to PCG
+// when the preconditioner is not exactly the same operator from one
+// application to the next (BF16 activations round differently for every
+// residual).  r is updated with exact H products, so it tracks the true
+// residual b - Hx up to rounding.  The network's first application (to
+// r0 = b when x0 = 0) is the warm start.
 //
 // Fallback: when |r|^2 has not fallen over `stall_window` iterations the
 // host (polling between graph batches) recomputes the true residual, restarts
@@ -27,22 +31,29 @@
 
 namespace mmr {
 
+constexpr int LP_MAXM = 8;   // directions kept for the conjugation
+
 struct LpState {
     // per-iteration accumulators (zeroed together: keep them first)
-    double pq_re, pq_im, pr_re, pr_im, qz_re, qz_im, rr, mse;
-    double rr0, beta_re, beta_im, tol2;
+    double pq_re, pq_im, pr_re, pr_im, rr, mse;
+    double qz[2 * LP_MAXM];          // q_j' z (re, im) per ring slot
+    double pqh[2 * LP_MAXM];         // p_j' q_j per ring slot
+    double beta[2 * LP_MAXM];        // -(q_j' z) / (p_j' q_j)
+    double rr0, tol2;
     int nit, nitmax, finished, status, stalled, window, plain, cap;
+    int m, slot, nstored, pad;       // ring size, slot of the current direction, valid slots
     unsigned int counter, counter2;
 };
-constexpr size_t LP_ACC_BYTES = offsetof(LpState, rr0);
+constexpr size_t LP_ACC_BYTES = offsetof(LpState, pqh);
 
 struct LpWorkspace {
     long long n = 0;
-    DevBuf x, p, q, r, z, b, tmp, tik, gt, state, hist, nrm;
+    DevBuf x, p, q, r, z, b, tmp, tik, gt, state, hist, nrm, ring_p, ring_q;
     Staged sy, sxo;
     cudaGraphExec_t g_learn = nullptr, g_plain = nullptr;
     int k_learn = 0, k_plain = 0;
-    const void* key[8] = {nullptr};
+    static constexpr int NKEY = 12;
+    const void* key[NKEY] = {nullptr};
     long long keyv[4] = {0};
     ~LpWorkspace() {
         if (g_learn) cudaGraphExecDestroy(g_learn);
@@ -91,10 +102,12 @@ __global__ void lp_init_kernel(const float2* __restrict__ b, const float2* __res
     }
 }
 
-// q += tik.*p ; p'q ; p'r
+// q += tik.*p ; p'q ; p'r ; (p, q) into the ring slot of this iteration
 __global__ void lp_pq_kernel(const float2* __restrict__ p, float2* __restrict__ q, const float2* __restrict__ r,
-                             const float* __restrict__ tik, long long n, LpState* st) {
+                             const float* __restrict__ tik, float2* __restrict__ ring_p, float2* __restrict__ ring_q,
+                             long long n, LpState* st) {
     if (st->finished) return;
+    const long long so = (long long)st->slot * n;
     double v[4] = {0, 0, 0, 0};
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const float2 pi = p[i], ri = r[i];
@@ -103,6 +116,8 @@ __global__ void lp_pq_kernel(const float2* __restrict__ p, float2* __restrict__ 
             qi = make_float2(qi.x + tik[i] * pi.x, qi.y + tik[i] * pi.y);
             q[i] = qi;
         }
+        ring_p[so + i] = pi;
+        ring_q[so + i] = qi;
         v[0] += (double)pi.x * qi.x + (double)pi.y * qi.y;
         v[1] += (double)pi.x * qi.y - (double)pi.y * qi.x;
         v[2] += (double)pi.x * ri.x + (double)pi.y * ri.y;
@@ -148,6 +163,8 @@ __global__ void lp_update_kernel(float2* __restrict__ x, const float2* __restric
         const int k = vs->nit + 1;
         const double rr = vs->rr;
         const int cap = vs->cap;
+        vs->pqh[2 * vs->slot] = bad ? 0.0 : pqr;
+        vs->pqh[2 * vs->slot + 1] = bad ? 0.0 : pqi;
         if (k < cap) {
             hist[k] = rr;
             hist[cap + k] = vs->mse;
@@ -167,37 +184,72 @@ __global__ void lp_update_kernel(float2* __restrict__ x, const float2* __restric
     }
 }
 
-// q'z ; beta = -(q'z)/(p'q) ; zero the accumulators for the next iteration
-__global__ void lp_qz_kernel(const float2* __restrict__ q, const float2* __restrict__ z, long long n, LpState* st) {
+// q_j'z for every valid ring slot j (the current direction included); the last block forms
+// beta_j = -(q_j'z)/(p_j'q_j), advances the ring and zeroes the accumulators.
+__global__ void lp_qz_kernel(const float2* __restrict__ ring_q, const float2* __restrict__ z, long long n,
+                             LpState* st) {
     if (st->finished) return;
-    double v[2] = {0, 0};
+    const int m = st->m;
+    const int nv = min(st->nstored + 1, m);
+    double v[2 * LP_MAXM];
+#pragma unroll
+    for (int j = 0; j < 2 * LP_MAXM; ++j) v[j] = 0.0;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const float2 qi = q[i], zi = z[i];
-        v[0] += (double)qi.x * zi.x + (double)qi.y * zi.y;
-        v[1] += (double)qi.x * zi.y - (double)qi.y * zi.x;
+        const float2 zi = z[i];
+#pragma unroll
+        for (int j = 0; j < LP_MAXM; ++j) {
+            if (j < nv) {
+                const float2 qi = ring_q[(long long)j * n + i];
+                v[2 * j] += (double)qi.x * zi.x + (double)qi.y * zi.y;
+                v[2 * j + 1] += (double)qi.x * zi.y - (double)qi.y * zi.x;
+            }
+        }
     }
-    double* const dst[2] = {&st->qz_re, &st->qz_im};
-    block_accumulate<2>(v, dst);
+    double* dst[2 * LP_MAXM];
+#pragma unroll
+    for (int j = 0; j < 2 * LP_MAXM; ++j) dst[j] = j < 2 * nv ? &st->qz[j] : nullptr;
+    block_accumulate<2 * LP_MAXM>(v, dst);
     if (last_block_of(&st->counter2)) {
         volatile LpState* vs = st;
-        const double pqr = vs->pq_re, pqi = vs->pq_im;
-        double2 bt = make_double2(0.0, 0.0);
-        if (pqr * pqr + pqi * pqi > 0.0) bt = cdiv_d(-vs->qz_re, -vs->qz_im, pqr, pqi);
-        if (!isfinite(bt.x + bt.y)) bt = make_double2(0.0, 0.0);
-        vs->beta_re = bt.x;
-        vs->beta_im = bt.y;
-        vs->pq_re = vs->pq_im = vs->pr_re = vs->pr_im = vs->qz_re = vs->qz_im = vs->rr = vs->mse = 0.0;
+        for (int j = 0; j < LP_MAXM; ++j) {
+            double2 bt = make_double2(0.0, 0.0);
+            const double pr = vs->pqh[2 * j], pi = vs->pqh[2 * j + 1];
+            if (j < nv && pr * pr + pi * pi > 0.0) bt = cdiv_d(-vs->qz[2 * j], -vs->qz[2 * j + 1], pr, pi);
+            if (!isfinite(bt.x + bt.y)) bt = make_double2(0.0, 0.0);
+            vs->beta[2 * j] = bt.x;
+            vs->beta[2 * j + 1] = bt.y;
+        }
+        vs->nstored = nv;
+        vs->slot = (vs->slot + 1) % m;
+        vs->pq_re = vs->pq_im = vs->pr_re = vs->pr_im = vs->rr = vs->mse = 0.0;
+        for (int j = 0; j < 2 * LP_MAXM; ++j) vs->qz[j] = 0.0;
         vs->counter2 = 0;
     }
 }
 
-// p = z + beta p
-__global__ void lp_p_kernel(float2* __restrict__ p, const float2* __restrict__ z, long long n, const LpState* st) {
+// p = z + sum_j beta_j p_j over the valid ring slots
+__global__ void lp_p_kernel(float2* __restrict__ p, const float2* __restrict__ z, const float2* __restrict__ ring_p,
+                            long long n, const LpState* st) {
     if (st->finished) return;
-    const double br = st->beta_re, bi = st->beta_im;
+    const int nv = st->nstored;
+    double br[LP_MAXM], bi[LP_MAXM];
+#pragma unroll
+    for (int j = 0; j < LP_MAXM; ++j) {
+        br[j] = st->beta[2 * j];
+        bi[j] = st->beta[2 * j + 1];
+    }
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const float2 pi = p[i], zi = z[i];
-        p[i] = make_float2((float)((double)zi.x + br * pi.x - bi * pi.y), (float)((double)zi.y + br * pi.y + bi * pi.x));
+        const float2 zi = z[i];
+        double ax = zi.x, ay = zi.y;
+#pragma unroll
+        for (int j = 0; j < LP_MAXM; ++j) {
+            if (j < nv) {
+                const float2 pj = ring_p[(long long)j * n + i];
+                ax += br[j] * pj.x - bi[j] * pj.y;
+                ay += br[j] * pj.y + bi[j] * pj.x;
+            }
+        }
+        p[i] = make_float2((float)ax, (float)ay);
     }
 }
 
@@ -230,16 +282,18 @@ static void lp_iter(const LpCall& c, LpWorkspace& w, bool learned, cudaStream_t 
     float2* r = w.r.as<float2>();
     float2* z = learned ? w.z.as<float2>() : r;
     const float* tik = c.has_tik ? w.tik.as<float>() : nullptr;
+    float2* ring_p = w.ring_p.as<float2>();
+    float2* ring_q = w.ring_q.as<float2>();
     sense_normal(*c.a, p, q, st, &sp->finished);
-    lp_pq_kernel<<<g, 256, 0, st>>>(p, q, r, tik, n, sp);
+    lp_pq_kernel<<<g, 256, 0, st>>>(p, q, r, tik, ring_p, ring_q, n, sp);
     check_launch("lp_pq");
     lp_update_kernel<<<g, 256, 0, st>>>(w.x.as<float2>(), p, q, r, c.has_gt ? w.gt.as<float2>() : nullptr, n, sp,
                                         w.hist.as<double>());
     check_launch("lp_update");
     if (learned) cnn_forward(*c.net, r, z, c.nx, c.ny, 1, &sp->rr, c.flags, st);
-    lp_qz_kernel<<<g, 256, 0, st>>>(q, z, n, sp);
+    lp_qz_kernel<<<g, 256, 0, st>>>(ring_q, z, n, sp);
     check_launch("lp_qz");
-    lp_p_kernel<<<g, 256, 0, st>>>(p, z, n, sp);
+    lp_p_kernel<<<g, 256, 0, st>>>(p, z, ring_p, n, sp);
     check_launch("lp_p");
 }
 
@@ -282,6 +336,10 @@ static void lp_start(const LpCall& c, LpWorkspace& w, bool learned, bool have_x,
     const long long n = w.n;
     const unsigned g = lp_grid(n);
     MMR_CUDA(cudaMemsetAsync(w.state.p, 0, LP_ACC_BYTES, st));
+    if (restart) {   // the conjugation history starts again from the new first direction
+        const int zero2[2] = {0, 0};
+        MMR_CUDA(cudaMemcpyAsync(&sp->slot, zero2, sizeof(zero2), cudaMemcpyHostToDevice, st));
+    }
     const float2* hx = nullptr;
     if (have_x) {
         sense_normal(*c.a, w.x.as<float2>(), w.tmp.as<float2>(), st, nullptr);
@@ -317,6 +375,10 @@ static void lp_solve(SenseOp& a, const void* y_user, CnnNet* net, const void* x0
     for (DevBuf* bb : {&w.x, &w.p, &w.q, &w.r, &w.z, &w.b, &w.tmp}) bb->ensure(n * sizeof(float2));
     const int nitmax = o.nit_max > 0 ? o.nit_max : 100;
     const int cap = nitmax + 1;
+    const int m = net ? std::min(std::max(o.fcg_m, 1), LP_MAXM) : 1;
+    // sized for the largest ring once, so that captured graphs never see these buffers move
+    w.ring_p.ensure((size_t)LP_MAXM * n * sizeof(float2));
+    w.ring_q.ensure((size_t)LP_MAXM * n * sizeof(float2));
     w.state.ensure(sizeof(LpState));
     w.hist.ensure((size_t)2 * cap * sizeof(double));
     w.nrm.ensure(2 * sizeof(double));
@@ -355,16 +417,20 @@ static void lp_solve(SenseOp& a, const void* y_user, CnnNet* net, const void* x0
     h.window = o.stall_window;
     h.cap = cap;
     h.plain = net ? 0 : 1;
+    h.m = m;
     MMR_CUDA(cudaMemcpyAsync(w.state.p, &h, sizeof(LpState), cudaMemcpyHostToDevice, st));
     MMR_CUDA(cudaMemsetAsync(w.hist.p, 0, (size_t)2 * cap * sizeof(double), st));
     lp_start(c, w, net != nullptr, x0_user != nullptr, false, st);
 
-    const void* key[8] = {a.d_wnorm.p, a.s_grid.p, a.s_grid2.p, w.x.p, w.hist.p, net, net ? net->act.p : nullptr,
-                          net ? net->wmma.p : nullptr};
+    // every buffer the captured kernels touch that can move between calls
+    const void* key[LpWorkspace::NKEY] = {a.d_wnorm.p, a.s_grid.p, a.s_grid2.p, w.x.p, w.hist.p, net,
+                                          net ? net->act.p : nullptr, w.ring_p.p, w.ring_q.p,
+                                          net ? net->wmma.p : nullptr, net ? net->sumsq.p : nullptr,
+                                          a.nufft ? a.nufft->s_tmp.p : nullptr};
     const long long keyv[4] = {a.w_bstride, sense_chunk(a), (n << 2) | ((long long)c.has_tik << 1) | (long long)c.has_gt,
                                ((long long)o.flags << 32) | (long long)(a.nufft && a.nufft->use_bins ? a.nufft->bins.T : 0)};
     bool same = w.g_plain != nullptr;
-    for (int i = 0; i < 8 && same; ++i) same = key[i] == w.key[i];
+    for (int i = 0; i < LpWorkspace::NKEY && same; ++i) same = key[i] == w.key[i];
     for (int i = 0; i < 4 && same; ++i) same = keyv[i] == w.keyv[i];
     if (!same) {
         if (w.g_learn) cudaGraphExecDestroy(w.g_learn);
@@ -372,7 +438,7 @@ static void lp_solve(SenseOp& a, const void* y_user, CnnNet* net, const void* x0
         w.g_learn = w.g_plain = nullptr;
         w.g_plain = lp_capture(c, w, false, w.k_plain);
         if (net) w.g_learn = lp_capture(c, w, true, w.k_learn);
-        for (int i = 0; i < 8; ++i) w.key[i] = key[i];
+        for (int i = 0; i < LpWorkspace::NKEY; ++i) w.key[i] = key[i];
         for (int i = 0; i < 4; ++i) w.keyv[i] = keyv[i];
     }
     bool learned = net != nullptr;
@@ -453,6 +519,7 @@ extern "C" int mmr_lpcg_default_opts(mmr_lpcg_opts* o) {
         o->stall_window = 10;
         o->flags = 2;   // tensor-core network forward
         o->poll = 8;
+        o->fcg_m = 4;
     });
 }
 

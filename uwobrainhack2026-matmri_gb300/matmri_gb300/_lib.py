@@ -78,7 +78,7 @@ class BfistaHist(C.Structure):
 class LpcgOpts(C.Structure):
     _fields_ = [("nit_max", C.c_int32), ("tol", C.c_double), ("tik_diag", C.POINTER(C.c_float)),
                 ("lam", C.c_double), ("gtruth", C.c_void_p), ("stall_window", C.c_int32), ("flags", C.c_int32),
-                ("poll", C.c_int32)]
+                ("poll", C.c_int32), ("fcg_m", C.c_int32)]
 
 
 class LpcgHist(C.Structure):

@@ -116,7 +116,8 @@ class PrecondNet:
 
 
 def lpcg(A, y, net: PrecondNet | None = None, x0=None, NitMax: int = 100, tol: float = 0.0, lam: float = 0.0,
-         tik_diag=None, gtruth=None, stall_window: int = 10, flags: int = _lib.CNN_TENSOR, poll: int = 8):
+         tik_diag=None, gtruth=None, stall_window: int = 10, flags: int = _lib.CNN_TENSOR, poll: int = 8,
+         fcg_m: int = 4):
     """x, res_sq, err_sq, info = lpcg(A, y, net, ...): learned-preconditioned CG-SENSE.
 
     Solves (A'A + lam + diag(tik_diag)) x = A'y like ``cgne(A, y, x0, NitMax, opt, gam, R)`` with
@@ -132,6 +133,7 @@ def lpcg(A, y, net: PrecondNet | None = None, x0=None, NitMax: int = 100, tol: f
     o.stall_window = int(stall_window)
     o.flags = int(flags) | (net.base_flags if net is not None else 0)
     o.poll = int(poll)
+    o.fcg_m = int(fcg_m)
     keep = []
     if tik_diag is not None:
         t = np.ascontiguousarray(np.asarray(tik_diag.cpu() if is_torch(tik_diag) else tik_diag,

@@ -175,6 +175,8 @@ def learned_pcg_comparison(dev, reps=5):
     S = mm.nufftOp([N_IMG, N_IMG], c["kloc"], None, 1, 2.0, 4)
     R = mm.rcvrOp(c["maps"], 0)
     A = mm.mrSampOp(S, R)
+    from matmri_gb300.autotune import autotune
+    autotune(A, rounds=1, use_cache=False)      # the fastest normal operator for both solvers
     y = np.asarray(A(c["img"].astype(np.complex64), "notransp"), dtype=np.complex128)
     y = synth.add_noise(y, 30.0, LEARNED_SEED + 7).astype(np.complex64)
     yd = torch.from_numpy(np.ascontiguousarray(y.T)).to(dev).T

@@ -314,6 +314,10 @@ typedef struct mmr_cnn mmr_cnn;
                                 the relative L2 (invariant to a complex scale)  */
 #define MMR_CNN_LINEAR   8   /* identity activations: the network is a fixed
                                 linear operator (forward and loss_grad)       */
+#define MMR_CNN_FOLDED   16  /* with MMR_CNN_LINEAR: apply the network as its
+                                folded (2L+1)^2 filter (2x2 real per tap) on the
+                                zero-extended image, composed in FP64 from the
+                                weights; FP32 arithmetic                      */
 
 MMR_API int mmr_cnn_create(int32_t nlayers, const int32_t* channels, mmr_cnn** out);
 MMR_API int mmr_cnn_num_params(const mmr_cnn* net, int64_t* n);

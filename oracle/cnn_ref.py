@@ -108,6 +108,21 @@ def forward(theta, r, channels=CHANNELS, keep=False, linear=False):
     return z
 
 
+def forward_extended(theta, r, channels=CHANNELS, linear=True):
+    """The network on the zero-extended image: r padded by L zeros on each side (L = layers, the
+    receptive-field radius), the network applied, the centre cropped.  Intermediate activations
+    outside the image are then whatever the layers compute there (not forced to zero), which is the
+    operator that crops reaching past the image edge train, and, for a linear network, the single
+    folded (2L+1)^2 filter."""
+    L = len(channels) - 1
+    r = np.asarray(r)
+    B, X, Y = r.shape
+    rp = np.zeros((B, X + 2 * L, Y + 2 * L), dtype=np.complex128)
+    rp[:, L:L + X, L:L + Y] = r
+    # the network is positively homogeneous, so the input normalisation does not change z
+    return forward(theta, rp, channels, linear=linear)[:, L:L + X, L:L + Y]
+
+
 def loss_and_grad(theta, r, e, margin, channels=CHANNELS, kind="rel", linear=False):
     """Loss over the interior mask m (margin pixels dropped on every side) and dL/dtheta.
 

@@ -136,7 +136,9 @@ def test_lpcg_learned_matches_oracle(mm, linear, m):
     theta = cnn_ref.init_params(21) * 0.3
     theta[-1] = 0.02
     net = PrecondNet(theta, linear=linear)
-    pre = lambda r: cnn_ref.forward(theta.astype(np.float64), r[None], linear=linear)[0]
+    # a linear network runs as its folded filter (the network on the zero-extended image)
+    fwd = cnn_ref.forward_extended if linear else cnn_ref.forward
+    pre = lambda r: fwd(theta.astype(np.float64), r[None], linear=linear)[0]
     lam = 0.5
     x, res, _, info = lpcg(A, y, net, NitMax=10, lam=lam, flags=_lib.CNN_FP32_ACT, stall_window=0, fcg_m=m)
     xr, res_r, _ = cnn_ref.fcg_ref(normal, b, pre, 10, lam=lam, m=m)
@@ -207,5 +209,25 @@ def test_trained_network_gain(mm):
     _, _, e_learn, info = lpcg(A, yd, net, NitMax=120, lam=lam, gtruth=xs)
     k_plain, k_learn = iterations_to(e_plain, gn), iterations_to(e_learn, gn)
     assert k_plain is not None and k_learn is not None
-    assert info["fell_back_at"] == -1
-    assert k_learn <= 0.7 * k_plain, (k_learn, k_plain)
+    assert info["fell_back_at"] == -1 or info["fell_back_at"] > k_learn
+    assert k_learn <= 0.5 * k_plain, (k_learn, k_plain)
+
+
+@pytest.mark.parametrize("shape", [(20, 17, 2), (256, 256, 1)])
+def test_folded_forward_matches_oracle(mm, shape):
+    """A linear network applied as its folded 13 x 13 filter equals the network on the
+    zero-extended image (the operator crop training optimises), to FP32 rounding."""
+    from matmri_gb300.learned import PrecondNet
+    from matmri_gb300 import _lib
+    rng = np.random.default_rng(6)
+    theta = cnn_ref.init_params(31)
+    theta[-1] = 0.3
+    net = PrecondNet(theta, linear=True)
+    r, rb = _batch(rng, *shape)
+    ref = np.moveaxis(cnn_ref.forward_extended(theta.astype(np.float64), rb, linear=True), 0, 2)
+    assert rel(net(r, _lib.CNN_FOLDED), ref) < 1e-5
+    # and it tracks weight updates (the fold is recomputed when the parameters change)
+    theta2 = theta * 1.1
+    net.set_params(theta2)
+    ref2 = np.moveaxis(cnn_ref.forward_extended(theta2.astype(np.float64), rb, linear=True), 0, 2)
+    assert rel(net(r, _lib.CNN_FOLDED), ref2) < 1e-5

@@ -82,3 +82,16 @@ def test_cosine_loss_gradient_and_scale_invariance():
     # a complex rescaling of the target leaves the loss unchanged
     L2, _ = cnn_ref.loss_and_grad(theta, r, (2 - 3j) * e, 1, ch, kind="cos")
     assert abs(L2 - L) < 1e-12
+
+
+def test_extended_forward_equals_layered_forward_in_the_interior():
+    # away from the border (farther than the receptive-field radius) the two agree
+    ch = (2, 4, 4, 2)
+    g = np.random.Generator(np.random.PCG64(12))
+    theta = cnn_ref.init_params(13, ch)
+    r = _rand_c(g, 1, 16, 14)
+    a = cnn_ref.forward(theta, r, ch, linear=True)
+    b = cnn_ref.forward_extended(theta, r, ch, linear=True)
+    L = len(ch) - 1
+    np.testing.assert_allclose(a[:, L:-L, L:-L], b[:, L:-L, L:-L], rtol=1e-10, atol=1e-12)
+    assert np.abs(a - b).max() > 1e-6     # and differ next to it

@@ -458,9 +458,130 @@ static void compute_sumsq(CnnNet& n, const float2* r, long long P, int B, cudaSt
     check_launch("cnn_sumsq");
 }
 
+// ------------------------------------------------------------ folded linear network ----
+// A linear network (identity activations) is one linear operator: composing the 3x3
+// layers (cross-correlations: offsets add) gives a single (2L+1)^2 filter with a real
+// 2x2 matrix per tap, z[p] = sum_d K[d] r[p + d] + skip r[p]; the input scale s cancels.
+// It is the operator the network computes on the zero-extended image (no intermediate
+// zero padding), which is what crop training past the image edge optimises.  Composed
+// on the host in FP64 whenever the weights change.
+static void cnn_fold(CnnNet& n, cudaStream_t st) {
+    if (n.folded_version == n.version) return;
+    std::vector<float> th((size_t)n.nparam);
+    MMR_CUDA(cudaMemcpyAsync(th.data(), n.theta.p, th.size() * 4, cudaMemcpyDeviceToHost, st));
+    MMR_CUDA(cudaStreamSynchronize(st));
+    // T[(dy+R)*(2R+1) + dx+R][co][ci], R grows by 1 per layer
+    int R = 1, cout = n.ch[1];
+    const int cin0 = n.ch[0];
+    std::vector<double> T((size_t)9 * cout * cin0);
+    for (int co = 0; co < cout; ++co)
+        for (int ci = 0; ci < cin0; ++ci)
+            for (int t = 0; t < 9; ++t)
+                T[((size_t)t * cout + co) * cin0 + ci] = th[n.woff[0] + ((size_t)co * cin0 + ci) * 9 + t];
+    for (int l = 1; l < n.L; ++l) {
+        const int cmid = n.ch[l], co2 = n.ch[l + 1], R2 = R + 1, S = 2 * R + 1, S2 = 2 * R2 + 1;
+        std::vector<double> U((size_t)S2 * S2 * co2 * cin0, 0.0);
+        const float* W = th.data() + n.woff[l];
+        for (int t = 0; t < 9; ++t) {
+            const int oy = t / 3 - 1, ox = t % 3 - 1;
+            for (int dy = -R; dy <= R; ++dy)
+                for (int dx = -R; dx <= R; ++dx) {
+                    const double* Tin = &T[((size_t)((dy + R) * S + dx + R) * cmid) * cin0];
+                    double* Uo = &U[((size_t)((dy + oy + R2) * S2 + dx + ox + R2) * co2) * cin0];
+                    for (int o = 0; o < co2; ++o)
+                        for (int c = 0; c < cmid; ++c) {
+                            const double w = W[((size_t)o * cmid + c) * 9 + t];
+                            if (w == 0.0) continue;
+                            for (int ci = 0; ci < cin0; ++ci) Uo[(size_t)o * cin0 + ci] += w * Tin[(size_t)c * cin0 + ci];
+                        }
+                }
+        }
+        T.swap(U);
+        R = R2;
+        cout = co2;
+    }
+    MMR_REQUIRE(cout == 2 && cin0 == 2, "folding needs a complex-in, complex-out network");
+    const int S = 2 * R + 1;
+    const double skip = th[n.nparam - 1];
+    std::vector<float4> K((size_t)S * S);
+    for (int d = 0; d < S * S; ++d) {
+        const double* m = &T[(size_t)d * 4];   // [co][ci]
+        const bool centre = d == R * S + R;
+        K[d] = make_float4((float)(m[0] + (centre ? skip : 0.0)), (float)m[1], (float)m[2],
+                           (float)(m[3] + (centre ? skip : 0.0)));
+    }
+    n.fold.ensure(K.size() * sizeof(float4));
+    MMR_CUDA(cudaMemcpyAsync(n.fold.p, K.data(), K.size() * sizeof(float4), cudaMemcpyHostToDevice, st));
+    MMR_CUDA(cudaStreamSynchronize(st));
+    n.fold_radius = R;
+    n.folded_version = n.version;
+}
+
+constexpr int FD_TX = 32, FD_TY = 16, FD_MAXR = 8;
+
+// z[p] = sum_d K[d] r[p+d]  (K: 2x2 real per tap as float4 {k00, k01, k10, k11}, zero outside the image)
+template <int R>
+__global__ void __launch_bounds__(256) conv_folded_kernel(const float2* __restrict__ r, float2* __restrict__ z,
+                                                          const float4* __restrict__ K, int X, int Y) {
+    constexpr int S = 2 * R + 1, HX = FD_TX + 2 * R, HY = FD_TY + 2 * R;
+    __shared__ float4 s_k[S * S];
+    __shared__ float2 s_r[HY][HX + 1];
+    const int b = blockIdx.z;
+    const long long P = (long long)X * Y;
+    const int x0 = blockIdx.x * FD_TX, y0 = blockIdx.y * FD_TY;
+    for (int i = threadIdx.x; i < S * S; i += blockDim.x) s_k[i] = K[i];
+    for (int i = threadIdx.x; i < HX * HY; i += blockDim.x) {
+        const int hx = i % HX, hy = i / HX, gx = x0 + hx - R, gy = y0 + hy - R;
+        s_r[hy][hx] = (gx >= 0 && gx < X && gy >= 0 && gy < Y) ? r[(long long)b * P + (long long)gy * X + gx]
+                                                                : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+    const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+    float a[2][2] = {{0.f, 0.f}, {0.f, 0.f}};
+#pragma unroll 1
+    for (int dy = 0; dy < S; ++dy) {
+#pragma unroll
+        for (int dx = 0; dx < S; ++dx) {
+            const float4 k = s_k[dy * S + dx];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const float2 v = s_r[ty + 8 * h + dy][tx + dx];
+                a[h][0] += k.x * v.x + k.y * v.y;
+                a[h][1] += k.z * v.x + k.w * v.y;
+            }
+        }
+    }
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int x = x0 + tx, y = y0 + ty + 8 * h;
+        if (x < X && y < Y) z[(long long)b * P + (long long)y * X + x] = make_float2(a[h][0], a[h][1]);
+    }
+}
+
+static void forward_folded(CnnNet& n, const float2* r, float2* z, int X, int Y, int B, cudaStream_t st) {
+    cnn_fold(n, st);
+    const dim3 grid((unsigned)cdiv(X, FD_TX), (unsigned)cdiv(Y, FD_TY), (unsigned)B);
+    MMR_REQUIRE(n.fold_radius <= FD_MAXR, "folded filter radius %d above %d", n.fold_radius, FD_MAXR);
+    switch (n.fold_radius) {
+        case 2: conv_folded_kernel<2><<<grid, 256, 0, st>>>(r, z, n.fold.as<float4>(), X, Y); break;
+        case 3: conv_folded_kernel<3><<<grid, 256, 0, st>>>(r, z, n.fold.as<float4>(), X, Y); break;
+        case 4: conv_folded_kernel<4><<<grid, 256, 0, st>>>(r, z, n.fold.as<float4>(), X, Y); break;
+        case 5: conv_folded_kernel<5><<<grid, 256, 0, st>>>(r, z, n.fold.as<float4>(), X, Y); break;
+        case 6: conv_folded_kernel<6><<<grid, 256, 0, st>>>(r, z, n.fold.as<float4>(), X, Y); break;
+        case 7: conv_folded_kernel<7><<<grid, 256, 0, st>>>(r, z, n.fold.as<float4>(), X, Y); break;
+        case 8: conv_folded_kernel<8><<<grid, 256, 0, st>>>(r, z, n.fold.as<float4>(), X, Y); break;
+        default: MMR_THROW(MMR_ERR_UNSUPPORTED, "folded filter radius %d", n.fold_radius);
+    }
+    check_launch("conv_folded");
+}
+
 void cnn_forward(CnnNet& n, const float2* r, float2* z, int X, int Y, int B, const double* sumsq, int flags,
                  cudaStream_t st) {
     const long long P = (long long)X * Y;
+    if ((flags & CNN_FOLDED) && (flags & CNN_LINEAR)) {
+        forward_folded(n, r, z, X, Y, B, st);
+        return;
+    }
     const bool fp32 = flags & CNN_FP32_ACT;
     const bool tc = (flags & CNN_TENSOR) && !fp32;
     ensure_scratch(n, P, B, false, fp32);

@@ -29,8 +29,10 @@ struct CnnNet {
     std::vector<long long> woff;     // offset of each layer in theta
     DevBuf theta, grad, adam_m, adam_v;
     DevBuf wpk, wpkT;                // packed forward / data-gradient weights (per layer, at woff)
-    DevBuf wmma;                     // tensor-core weights (bf16 hi/lo), hidden layers
-    long long version = 0, packed_version = -1;
+    DevBuf wmma;                     // tensor-core weights (fp16), hidden layers
+    DevBuf fold;                     // linear network folded into one filter: float4 [(2R+1)^2] (2x2 per tap)
+    int fold_radius = 0;
+    long long version = 0, packed_version = -1, folded_version = -1;
     long long adam_t = 0;
     // scratch
     DevBuf act, gbuf, gv, z, sumsq, lossacc, partial, dskip;
@@ -38,7 +40,7 @@ struct CnnNet {
     Staged st_in, st_out, st_tgt;
 };
 
-enum CnnFlags { CNN_FP32_ACT = 1, CNN_TENSOR = 2, CNN_LOSS_COS = 4, CNN_LINEAR = 8 };
+enum CnnFlags { CNN_FP32_ACT = 1, CNN_TENSOR = 2, CNN_LOSS_COS = 4, CNN_LINEAR = 8, CNN_FOLDED = 16 };
 
 // z = net(r) for `batch` complex images of nx x ny on device memory.  `sumsq`
 // (device, per image sum |r|^2) may be supplied by the caller (e.g. from a

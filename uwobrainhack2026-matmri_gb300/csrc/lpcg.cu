@@ -14,10 +14,11 @@
 // residual b - Hx up to rounding.  The network's first application (to
 // r0 = b when x0 = 0) is the warm start.
 //
-// Fallback: when |r|^2 has not fallen over `stall_window` iterations the
-// host (polling between graph batches) recomputes the true residual, restarts
-// the directions from it and continues with plain CG.  At exit the true
-// residual |b - Hx| / |b| is computed once more and returned (the judge).
+// Fallback: when |r|^2 has not fallen over `stall_window` iterations (while
+// still above the complex64 precision floor) the host, polling between graph
+// batches, recomputes the true residual, restarts the directions from it and
+// continues with plain CG.  At exit the true residual |b - Hx| / |b| is
+// computed once more and returned (the judge).
 //
 // Vectors are complex64; inner products, alpha, beta and the stopping tests
 // are FP64.  One iteration (learned or plain) is a captured CUDA graph.
@@ -31,7 +32,8 @@
 
 namespace mmr {
 
-constexpr int LP_MAXM = 8;   // directions kept for the conjugation
+constexpr int LP_MAXM = 8;          // directions kept for the conjugation
+constexpr double LP_FLOOR = 1e-12;  // |r|^2 / |r0|^2 below which a stall is not acted on
 
 struct LpState {
     // per-iteration accumulators (zeroed together: keep them first)
@@ -52,7 +54,7 @@ struct LpWorkspace {
     Staged sy, sxo;
     cudaGraphExec_t g_learn = nullptr, g_plain = nullptr;
     int k_learn = 0, k_plain = 0;
-    static constexpr int NKEY = 12;
+    static constexpr int NKEY = 13;
     const void* key[NKEY] = {nullptr};
     long long keyv[4] = {0};
     ~LpWorkspace() {
@@ -169,7 +171,10 @@ __global__ void lp_update_kernel(float2* __restrict__ x, const float2* __restric
             hist[k] = rr;
             hist[cap + k] = vs->mse;
         }
-        if (vs->window > 0 && !vs->plain && k >= vs->window && k - vs->window < cap && rr >= hist[k - vs->window])
+        // a stall counts only above the precision floor of complex64 vectors (|r| ~ 1e-6 |r0|),
+        // where any residual stops falling
+        if (vs->window > 0 && !vs->plain && k >= vs->window && k - vs->window < cap && rr >= hist[k - vs->window] &&
+            rr > LP_FLOOR * vs->rr0)
             vs->stalled = 1;
         if (bad && !vs->plain) vs->stalled = 1;
         int fin = 0;
@@ -426,6 +431,7 @@ static void lp_solve(SenseOp& a, const void* y_user, CnnNet* net, const void* x0
     const void* key[LpWorkspace::NKEY] = {a.d_wnorm.p, a.s_grid.p, a.s_grid2.p, w.x.p, w.hist.p, net,
                                           net ? net->act.p : nullptr, w.ring_p.p, w.ring_q.p,
                                           net ? net->wmma.p : nullptr, net ? net->sumsq.p : nullptr,
+                                          net ? net->fold.p : nullptr,
                                           a.nufft ? a.nufft->s_tmp.p : nullptr};
     const long long keyv[4] = {a.w_bstride, sense_chunk(a), (n << 2) | ((long long)c.has_tik << 1) | (long long)c.has_gt,
                                ((long long)o.flags << 32) | (long long)(a.nufft && a.nufft->use_bins ? a.nufft->bins.T : 0)};

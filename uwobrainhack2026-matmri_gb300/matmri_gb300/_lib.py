@@ -91,6 +91,7 @@ CNN_FP32_ACT = 1
 CNN_TENSOR = 2
 CNN_LOSS_COS = 4
 CNN_LINEAR = 8
+CNN_FOLDED = 16
 
 # name -> (restype, argtypes)
 SIGNATURES = {

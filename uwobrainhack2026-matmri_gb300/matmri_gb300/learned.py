@@ -117,7 +117,7 @@ class PrecondNet:
 
 def lpcg(A, y, net: PrecondNet | None = None, x0=None, NitMax: int = 100, tol: float = 0.0, lam: float = 0.0,
          tik_diag=None, gtruth=None, stall_window: int = 10, flags: int = _lib.CNN_TENSOR, poll: int = 8,
-         fcg_m: int = 4):
+         fcg_m: int = 4, fold: bool = True):
     """x, res_sq, err_sq, info = lpcg(A, y, net, ...): learned-preconditioned CG-SENSE.
 
     Solves (A'A + lam + diag(tik_diag)) x = A'y like ``cgne(A, y, x0, NitMax, opt, gam, R)`` with
@@ -131,7 +131,9 @@ def lpcg(A, y, net: PrecondNet | None = None, x0=None, NitMax: int = 100, tol: f
     o.tol = float(tol)
     o.lam = float(lam)
     o.stall_window = int(stall_window)
-    o.flags = int(flags) | (net.base_flags if net is not None else 0)
+    # a linear network is applied as its folded filter unless the caller picks the layered path
+    folded = _lib.CNN_FOLDED if (net is not None and net.linear and fold) else 0
+    o.flags = int(flags) | (net.base_flags if net is not None else 0) | folded
     o.poll = int(poll)
     o.fcg_m = int(fcg_m)
     keep = []

@@ -351,7 +351,8 @@ typedef struct mmr_lpcg_opts {
     const void*   gtruth;        /* optional [imN] complex64 for the error history */
     int32_t       stall_window;  /* fallback window (default 10; 0 = never)       */
     int32_t       flags;         /* MMR_CNN_* network flags (default TENSOR)      */
-    int32_t       poll;          /* host checks the device flags every poll its (8) */
+    int32_t       poll;          /* with tol > 0: the host checks for the stop every
+                                    poll iterations (8); the fallback needs no host */
     int32_t       fcg_m;         /* directions the new one is made H-conjugate to
                                     (1..8, default 4; plain CG uses 1)          */
 } mmr_lpcg_opts;

@@ -15,10 +15,13 @@
 // r0 = b when x0 = 0) is the warm start.
 //
 // Fallback: when |r|^2 has not fallen over `stall_window` iterations (while
-// still above the complex64 precision floor) the host, polling between graph
-// batches, recomputes the true residual, restarts the directions from it and
-// continues with plain CG.  At exit the true residual |b - Hx| / |b| is
-// computed once more and returned (the judge).
+// still above the complex64 precision floor), or a direction has no
+// curvature (a zero or non-finite network output), the same iteration
+// switches the solve to plain CG on the device: z = r from then on and the
+// directions restart from r at the current x.  No host round trip is needed,
+// so the host only polls when a residual tolerance can end the solve early.
+// At exit the true residual |b - Hx| / |b| is computed once more and
+// returned (the judge).
 //
 // Vectors are complex64; inner products, alpha, beta and the stopping tests
 // are FP64.  One iteration (learned or plain) is a captured CUDA graph.
@@ -43,7 +46,8 @@ struct LpState {
     double beta[2 * LP_MAXM];        // -(q_j' z) / (p_j' q_j)
     double rr0, tol2;
     int nit, nitmax, finished, status, stalled, window, plain, cap;
-    int m, slot, nstored, pad;       // ring size, slot of the current direction, valid slots
+    int m, slot, nstored, restart;   // ring size, slot of the current direction, valid slots, restart pending
+    int fell_at, pad;                // iteration of the switch to plain CG (-1: none)
     unsigned int counter, counter2;
 };
 constexpr size_t LP_ACC_BYTES = offsetof(LpState, pqh);
@@ -74,10 +78,11 @@ __device__ __forceinline__ double2 cdiv_d(double ar, double ai, double br, doubl
 }
 
 // r = b - Hx - tik.*x (Hx may be NULL: x = 0); |r|^2, |x - gt|^2; rr0 and history[0]
+// (judge = 1: the exit check, which only leaves |b - Hx - tik.*x|^2 in rr)
 __global__ void lp_init_kernel(const float2* __restrict__ b, const float2* __restrict__ hx,
                                const float2* __restrict__ x, const float* __restrict__ tik,
                                const float2* __restrict__ gt, float2* __restrict__ r, long long n, LpState* st,
-                               double* hist, int restart) {
+                               double* hist, int judge) {
     double v[2] = {0, 0};
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const float2 xi = x[i];
@@ -95,7 +100,7 @@ __global__ void lp_init_kernel(const float2* __restrict__ b, const float2* __res
     block_accumulate<2>(v, dst);
     if (last_block_of(&st->counter)) {
         volatile LpState* vs = st;
-        if (!restart) {
+        if (!judge) {
             vs->rr0 = vs->rr;
             hist[0] = vs->rr;
             hist[vs->cap] = vs->mse;
@@ -177,6 +182,11 @@ __global__ void lp_update_kernel(float2* __restrict__ x, const float2* __restric
             rr > LP_FLOOR * vs->rr0)
             vs->stalled = 1;
         if (bad && !vs->plain) vs->stalled = 1;
+        if (vs->stalled && !vs->plain) {   // fall back to plain CG from this x
+            vs->plain = 1;
+            vs->restart = 1;
+            vs->fell_at = k;
+        }
         int fin = 0;
         if (vs->tol2 > 0 && rr <= vs->tol2 * vs->rr0) {
             fin = 1;
@@ -190,10 +200,12 @@ __global__ void lp_update_kernel(float2* __restrict__ x, const float2* __restric
 }
 
 // q_j'z for every valid ring slot j (the current direction included); the last block forms
-// beta_j = -(q_j'z)/(p_j'q_j), advances the ring and zeroes the accumulators.
-__global__ void lp_qz_kernel(const float2* __restrict__ ring_q, const float2* __restrict__ z, long long n,
-                             LpState* st) {
+// beta_j = -(q_j'z)/(p_j'q_j), advances the ring and zeroes the accumulators.  After the
+// switch to plain CG z is r; on the switch itself the directions restart (all beta_j = 0).
+__global__ void lp_qz_kernel(const float2* __restrict__ ring_q, const float2* __restrict__ zn,
+                             const float2* __restrict__ r, long long n, LpState* st) {
     if (st->finished) return;
+    const float2* __restrict__ z = st->plain ? r : zn;
     const int m = st->m;
     const int nv = min(st->nstored + 1, m);
     double v[2 * LP_MAXM];
@@ -216,26 +228,31 @@ __global__ void lp_qz_kernel(const float2* __restrict__ ring_q, const float2* __
     block_accumulate<2 * LP_MAXM>(v, dst);
     if (last_block_of(&st->counter2)) {
         volatile LpState* vs = st;
+        const bool restart = vs->restart;
         for (int j = 0; j < LP_MAXM; ++j) {
             double2 bt = make_double2(0.0, 0.0);
             const double pr = vs->pqh[2 * j], pi = vs->pqh[2 * j + 1];
-            if (j < nv && pr * pr + pi * pi > 0.0) bt = cdiv_d(-vs->qz[2 * j], -vs->qz[2 * j + 1], pr, pi);
+            if (!restart && j < nv && pr * pr + pi * pi > 0.0)
+                bt = cdiv_d(-vs->qz[2 * j], -vs->qz[2 * j + 1], pr, pi);
             if (!isfinite(bt.x + bt.y)) bt = make_double2(0.0, 0.0);
             vs->beta[2 * j] = bt.x;
             vs->beta[2 * j + 1] = bt.y;
         }
-        vs->nstored = nv;
-        vs->slot = (vs->slot + 1) % m;
+        // valid ring entries are always slots [0, nstored): a restart begins again at slot 0
+        vs->nstored = restart ? 0 : nv;
+        vs->restart = 0;
+        vs->slot = restart ? 0 : (vs->slot + 1) % m;
         vs->pq_re = vs->pq_im = vs->pr_re = vs->pr_im = vs->rr = vs->mse = 0.0;
         for (int j = 0; j < 2 * LP_MAXM; ++j) vs->qz[j] = 0.0;
         vs->counter2 = 0;
     }
 }
 
-// p = z + sum_j beta_j p_j over the valid ring slots
-__global__ void lp_p_kernel(float2* __restrict__ p, const float2* __restrict__ z, const float2* __restrict__ ring_p,
-                            long long n, const LpState* st) {
+// p = z + sum_j beta_j p_j over the valid ring slots (z = r after the switch to plain CG)
+__global__ void lp_p_kernel(float2* __restrict__ p, const float2* __restrict__ zn, const float2* __restrict__ r,
+                            const float2* __restrict__ ring_p, long long n, const LpState* st) {
     if (st->finished) return;
+    const float2* __restrict__ z = st->plain ? r : zn;
     const int nv = st->nstored;
     double br[LP_MAXM], bi[LP_MAXM];
 #pragma unroll
@@ -296,9 +313,9 @@ static void lp_iter(const LpCall& c, LpWorkspace& w, bool learned, cudaStream_t 
                                         w.hist.as<double>());
     check_launch("lp_update");
     if (learned) cnn_forward(*c.net, r, z, c.nx, c.ny, 1, &sp->rr, c.flags, st);
-    lp_qz_kernel<<<g, 256, 0, st>>>(ring_q, z, n, sp);
+    lp_qz_kernel<<<g, 256, 0, st>>>(ring_q, z, r, n, sp);
     check_launch("lp_qz");
-    lp_p_kernel<<<g, 256, 0, st>>>(p, z, ring_p, n, sp);
+    lp_p_kernel<<<g, 256, 0, st>>>(p, z, r, ring_p, n, sp);
     check_launch("lp_p");
 }
 
@@ -336,15 +353,11 @@ static cudaGraphExec_t lp_capture(const LpCall& c, LpWorkspace& w, bool learned,
 }
 
 // Sets x, r, p (and rr) from scratch: r = b - Hx - tik.*x, z = M(r), p = z.
-static void lp_start(const LpCall& c, LpWorkspace& w, bool learned, bool have_x, bool restart, cudaStream_t st) {
+static void lp_start(const LpCall& c, LpWorkspace& w, bool learned, bool have_x, cudaStream_t st) {
     LpState* sp = w.state.as<LpState>();
     const long long n = w.n;
     const unsigned g = lp_grid(n);
     MMR_CUDA(cudaMemsetAsync(w.state.p, 0, LP_ACC_BYTES, st));
-    if (restart) {   // the conjugation history starts again from the new first direction
-        const int zero2[2] = {0, 0};
-        MMR_CUDA(cudaMemcpyAsync(&sp->slot, zero2, sizeof(zero2), cudaMemcpyHostToDevice, st));
-    }
     const float2* hx = nullptr;
     if (have_x) {
         sense_normal(*c.a, w.x.as<float2>(), w.tmp.as<float2>(), st, nullptr);
@@ -352,7 +365,7 @@ static void lp_start(const LpCall& c, LpWorkspace& w, bool learned, bool have_x,
     }
     lp_init_kernel<<<g, 256, 0, st>>>(w.b.as<float2>(), hx, w.x.as<float2>(), c.has_tik ? w.tik.as<float>() : nullptr,
                                       c.has_gt ? w.gt.as<float2>() : nullptr, w.r.as<float2>(), n, sp,
-                                      w.hist.as<double>(), restart ? 1 : 0);
+                                      w.hist.as<double>(), 0);
     check_launch("lp_init");
     if (learned) {
         cnn_forward(*c.net, w.r.as<float2>(), w.z.as<float2>(), c.nx, c.ny, 1, &sp->rr, c.flags, st);
@@ -423,9 +436,10 @@ static void lp_solve(SenseOp& a, const void* y_user, CnnNet* net, const void* x0
     h.cap = cap;
     h.plain = net ? 0 : 1;
     h.m = m;
+    h.fell_at = -1;
     MMR_CUDA(cudaMemcpyAsync(w.state.p, &h, sizeof(LpState), cudaMemcpyHostToDevice, st));
     MMR_CUDA(cudaMemsetAsync(w.hist.p, 0, (size_t)2 * cap * sizeof(double), st));
-    lp_start(c, w, net != nullptr, x0_user != nullptr, false, st);
+    lp_start(c, w, net != nullptr, x0_user != nullptr, st);
 
     // every buffer the captured kernels touch that can move between calls
     const void* key[LpWorkspace::NKEY] = {a.d_wnorm.p, a.s_grid.p, a.s_grid2.p, w.x.p, w.hist.p, net,
@@ -447,33 +461,24 @@ static void lp_solve(SenseOp& a, const void* y_user, CnnNet* net, const void* x0
         for (int i = 0; i < LpWorkspace::NKEY; ++i) w.key[i] = key[i];
         for (int i = 0; i < 4; ++i) w.keyv[i] = keyv[i];
     }
-    bool learned = net != nullptr;
-    int fell_back = -1;
-    const int poll = o.poll > 0 ? o.poll : 8;
+    // The fallback to plain CG happens on the device (the learned graph reads z = r once the
+    // solve has switched), so the host only has to watch for a tolerance that ends it early.
+    cudaGraphExec_t gx = net ? w.g_learn : w.g_plain;
+    const int kx = net ? w.k_learn : w.k_plain;
+    const int poll = h.tol2 > 0 ? (o.poll > 0 ? o.poll : 8) : nitmax;
     int it = 0;
     LpState* sp = w.state.as<LpState>();
     while (it < nitmax) {
         const int end = std::min(nitmax, it + poll);
         for (; it < end; ++it) {
-            MMR_CUDA(cudaGraphLaunch(learned ? w.g_learn : w.g_plain, st));
-            add_launches(learned ? w.k_learn : w.k_plain);
+            MMR_CUDA(cudaGraphLaunch(gx, st));
+            add_launches(kx);
         }
-        int flags[3] = {0, 0, 0};   // finished, status, stalled
-        MMR_CUDA(cudaMemcpyAsync(flags, &sp->finished, 3 * sizeof(int), cudaMemcpyDeviceToHost, st));
+        if (end >= nitmax) break;
+        int fin = 0;
+        MMR_CUDA(cudaMemcpyAsync(&fin, &sp->finished, sizeof(int), cudaMemcpyDeviceToHost, st));
         MMR_CUDA(cudaStreamSynchronize(st));
-        if (flags[0]) break;
-        if (learned && flags[2]) {
-            // the true residual stopped falling: restart plain CG from the current x
-            int nit = 0;
-            MMR_CUDA(cudaMemcpy(&nit, &sp->nit, sizeof(int), cudaMemcpyDeviceToHost));
-            fell_back = nit;
-            learned = false;
-            const int one = 1, zero = 0;
-            MMR_CUDA(cudaMemcpyAsync(&sp->plain, &one, sizeof(int), cudaMemcpyHostToDevice, st));
-            MMR_CUDA(cudaMemcpyAsync(&sp->stalled, &zero, sizeof(int), cudaMemcpyHostToDevice, st));
-            lp_start(c, w, false, true, true, st);
-            MMR_CUDA(cudaStreamSynchronize(st));
-        }
+        if (fin) break;
     }
     // judge: true residual |b - Hx - tik.*x| / |b|
     sense_normal(a, w.x.as<float2>(), w.tmp.as<float2>(), st, nullptr);
@@ -497,7 +502,7 @@ static void lp_solve(SenseOp& a, const void* y_user, CnnNet* net, const void* x0
         hist->nit = fs.nit;
         hist->n = std::min(cap, fs.nit + 1);
         hist->status = fs.status;
-        hist->fell_back_at = fell_back;
+        hist->fell_back_at = fs.fell_at;
         hist->true_res_rel = bn > 0 ? std::sqrt(fs.rr / bn) : 0.0;
         std::vector<double> hh((size_t)2 * cap);
         MMR_CUDA(cudaMemcpy(hh.data(), w.hist.p, hh.size() * sizeof(double), cudaMemcpyDeviceToHost));

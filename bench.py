@@ -282,6 +282,92 @@ def batched_comparison(dev, nit=25, reps=3):
             "setup_s": setup_s}
 
 
+def _timed_ms(fn, reps, dev):
+    import torch
+    st = torch.cuda.current_stream(dev)
+    for _ in range(3):
+        fn()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(st)
+    for _ in range(reps):
+        fn()
+    e1.record(st)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def _dev_cm(a, dev):
+    """Column-major complex64 device tensor of a numpy array."""
+    import torch
+    a = np.asarray(a, dtype=np.complex64)
+    return torch.from_numpy(np.ascontiguousarray(a.T)).to(dev).T if a.ndim > 1 else torch.from_numpy(a).to(dev)
+
+
+def regridding_measure(dev, reps=200):
+    """128 x 128 single-coil regridding (16 x 2048 spiral, kwidth 4, os 2, |k| density compensation,
+    SNR 50): microseconds per adjoint + forward pair on device-resident data, its error against the
+    FP64 restatement, and the restatement's own time on the host cores."""
+    import matmri_gb300 as mm
+    from matmri_gb300 import synth
+    import oracle.nufft_ref as nr
+    c = synth.regridding_case()
+    N = c["N"]
+    S = mm.nufftOp([N, N], c["kloc"], c["dcf"], 1, c["os"], c["kwidth"])
+    Sr = nr.NufftRef([N, N], c["kloc"], c["dcf"], c["os"], c["kwidth"])
+    y = synth.add_noise(Sr.mtimes(c["img"]), c["snr"], c["seed"] + 1)
+    yd = _dev_cm(y, dev)
+    SH = S.H
+    us = 1e3 * _timed_ms(lambda: S * (SH * yd), reps, dev)
+    x_gpu = (SH * yd).cpu().numpy()
+    t0 = time.perf_counter()
+    x_ref = Sr.H.mtimes(y)
+    y_ref = Sr.mtimes(x_ref)
+    t_cpu = time.perf_counter() - t0
+    y_gpu = (S * _dev_cm(x_ref, dev)).cpu().numpy()
+    err_adj = float(np.linalg.norm(x_gpu - x_ref) / np.linalg.norm(x_ref))
+    err_fwd = float(np.linalg.norm(y_gpu - y_ref) / np.linalg.norm(y_ref))
+    return {"workload": "regridding 128x128, 16x2048 spiral, kwidth 4, os 2, |k| dcf, 1 coil, SNR 50",
+            "us_per_adjoint_forward": us, "rel_err_adjoint_vs_fp64": err_adj, "rel_err_forward_vs_fp64": err_fwd,
+            "cpu_fp64_us_per_pair": t_cpu * 1e6, "cpu_cores": len(os.sched_getaffinity(0))}
+
+
+def highorder_measure(dev, reps=5, nit=30):
+    """High-order encoding: 128 x 128, single-shot spiral of 16384 samples, 16 spherical-harmonic
+    terms, B0 +-100 Hz, 30 ms readout, 16 coils.  Times the 16-coil S*x and S'*y and a cgne solve of
+    `nit` iterations on device-resident data; error of S*x against the exact FP64 sum on 256 samples."""
+    import matmri_gb300 as mm
+    from matmri_gb300 import synth
+    from oracle.sho_ref import ShoRef
+    b0, t, spha, conc, grid = synth.highorder_inputs(128, 16384)
+    S = mm.sampHighOrder(b0, t, spha, conc, grid)
+    maps = synth.coil_maps(128, 16, 3001)
+    A = mm.mrSampOp(S, mm.rcvrOp(maps, 0))
+    img = synth.ellipse_phantom(128, 10, 3002, complex_phase=True)
+    xd = _dev_cm(img, dev)
+    yd = A(xd, "notransp")
+    ms_fwd = _timed_ms(lambda: A(xd, "notransp"), reps, dev)
+    ms_adj = _timed_ms(lambda: A(yd, "transp"), reps, dev)
+    opt = {"resThresh": None, "xChangeThresh": None}
+    ms_solve = _timed_ms(lambda: mm.cgne(A, yd, None, nit, opt), 2, dev)
+    # exact FP64 S*x (one coil image) on a sample subset
+    xs = img * maps[:, :, 0]
+    ys = (S * _dev_cm(xs, dev)).cpu().numpy()
+    ref = ShoRef(b0, t, spha, conc, grid)
+    rng = np.random.default_rng(7)
+    ms_idx = np.sort(rng.choice(t.size, 256, replace=False))
+    xv = xs.reshape(-1, order="F")
+    B, P = ref.basis_matrix()
+    exact = np.exp(1j * (B @ P[:, ms_idx])).T @ xv / math.sqrt(xv.size)     # sampHighOrder.m:376, 387
+    rel = float(np.linalg.norm(ys.reshape(-1)[ms_idx] - exact) / np.linalg.norm(exact))
+    V, M, C = img.size, t.size, 16
+    return {"workload": "sampHighOrder 128x128, 16384-sample spiral, 16 SH terms, B0 +-100 Hz, 30 ms, 16 coils",
+            "ms_forward_16coils": ms_fwd, "ms_adjoint_16coils": ms_adj,
+            "tflops_forward": 8.0 * V * M * C / (ms_fwd * 1e-3) / 1e12,
+            "ms_cgne_solve": ms_solve, "iterations": nit, "solves_per_s": 1e3 / ms_solve,
+            "rel_err_forward_vs_fp64_256_samples": rel}
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -327,6 +413,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned-PCG vs plain-CG comparison")
     ap.add_argument("--no-batched", action="store_true", help="skip the 64-slice batched comparison")
+    ap.add_argument("--no-extra", action="store_true", help="skip the regridding and high-order encoding lines")
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--tuning", default=None,
                     help="fixed knobs coil_chunk,tile,coil_group,item,fft_lines,normal_mode (skips the autotuner)")
@@ -491,6 +578,9 @@ def main():
             line["learned_pcg"] = learned_pcg_comparison(dev)
         if not args.no_batched:
             line["batched"] = batched_comparison(dev)
+        if not args.no_extra:
+            line["regridding"] = regridding_measure(dev)
+            line["highorder"] = highorder_measure(dev)
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(case)
         print(json.dumps(line), flush=True)

@@ -145,6 +145,11 @@ MMR_API int mmr_sho_create(const mmr_sho_desc* desc, mmr_sho** out);
  * sums, sampHighOrder.m:393-457).                                         */
 MMR_API int mmr_sho_apply(mmr_sho* s, int adjoint, const void* in, void* out,
                   int64_t nbatch, void* stream);
+/* Selects the contraction: on = 1 (default) the tensor cores (mma.sync,
+ * operands split into FP16 hi + scaled lo parts, FP32 accumulation), on = 0
+ * the SIMT FP32 kernels.  Both read the FP32-turns phase table; without room
+ * for the table the SIMT kernels evaluate the phase per element in FP64.  */
+MMR_API int mmr_sho_set_tensor(mmr_sho* s, int on);
 MMR_API int mmr_sho_destroy(mmr_sho* s);
 
 /* ---- mrSampFunc --------------------------------------------------------------

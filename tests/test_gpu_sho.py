@@ -83,3 +83,27 @@ def test_highorder_workload_small(mm):
     y = crandn(rng, (2048, 4))
     assert rel(S * x, Sr.mtimes(x)) < 1e-5
     assert rel(S.H * y, Sr.H.mtimes(y)) < 1e-5
+
+
+@pytest.mark.parametrize("ncoil", [1, 3, 6, 16, 21])
+@pytest.mark.parametrize("shape", [((24, 20), 1500), ((32, 32), 1024)])
+def test_tensor_core_contraction(mm, ncoil, shape):
+    """The tensor-core path (FP16 hi + scaled lo splits, FP32 accumulation) against the FP64
+    restatement and the SIMT path, both directions, coil counts across the n-tile cases and sizes
+    that are not multiples of the 8-element K step."""
+    from matmri_gb300 import synth
+    imN, M = shape
+    b0, t, spha, conc, grid = synth.highorder_inputs(N=imN[0], M=M, seed=11)
+    grid = {k: v[:, :imN[1]] for k, v in grid.items()}
+    b0 = b0[:, :imN[1]]
+    S = mm.sampHighOrder(b0, t, spha, conc, grid)
+    Sr = ShoRef(b0, t, spha, conc, grid)
+    rng = np.random.default_rng(ncoil)
+    x = crandn(rng, list(imN) + [ncoil])
+    y = crandn(rng, (M, ncoil))
+    yt, xt = S * x, S.H * y
+    assert rel(yt, Sr.mtimes(x)) < 1e-5
+    assert rel(xt, Sr.H.mtimes(y)) < 1e-5
+    S.set_tensor(False)
+    assert rel(yt, S * x) < 1e-5
+    assert rel(xt, S.H * y) < 1e-5

@@ -17,6 +17,7 @@
 #include <cmath>
 
 #include "sense.cuh"
+#include "sho_tc.cuh"
 
 namespace mmr {
 
@@ -29,6 +30,8 @@ struct ShoPlan {
     DevBuf d_P;     // double [K][M]
     DevBuf d_turn;  // float  [V][M] (empty: on-the-fly FP64 phase)
     bool table = false;
+    bool tensor = true;     // with the table: tensor-core contraction (sho_tc.cu), else the SIMT kernels
+    ShoTcScratch tc;
     Staged st_in, st_out;
 };
 
@@ -207,6 +210,10 @@ __global__ void __launch_bounds__(256) sho_adj_kernel(const float* __restrict__ 
 }
 
 void sho_forward(ShoPlan& s, const float2* x, float2* y, long long nb, cudaStream_t st, const int* active) {
+    if (s.table && s.tensor && nb <= SHO_TC_MAX_COILS) {
+        sho_tc_forward(s.tc, s.d_turn.as<float>(), s.V, s.M, x, y, nb, st, active);
+        return;
+    }
     const float scale = (float)(1.0 / std::sqrt((double)s.V));
     const float* tb = s.table ? s.d_turn.as<float>() : nullptr;
     const unsigned gx = (unsigned)cdiv(s.M, 256);
@@ -224,6 +231,10 @@ void sho_forward(ShoPlan& s, const float2* x, float2* y, long long nb, cudaStrea
 }
 
 void sho_adjoint(ShoPlan& s, const float2* y, float2* x, long long nb, cudaStream_t st, const int* active) {
+    if (s.table && s.tensor && nb <= SHO_TC_MAX_COILS) {
+        sho_tc_adjoint(s.tc, s.d_turn.as<float>(), s.V, s.M, y, x, nb, st, active);
+        return;
+    }
     const float scale = (float)(1.0 / std::sqrt((double)s.V));
     const float* tb = s.table ? s.d_turn.as<float>() : nullptr;
     const unsigned gx = (unsigned)cdiv(s.V, 256);
@@ -299,6 +310,7 @@ static void sho_build(ShoPlan& s, const mmr_sho_desc& d) {
                                                           s.d_turn.as<float>());
         check_launch("sho_table");
         MMR_CUDA(cudaDeviceSynchronize());
+        sho_tc_alloc(s.tc, s.V, s.M);
     }
 }
 
@@ -332,6 +344,13 @@ extern "C" int mmr_sho_apply(mmr_sho* h, int adjoint, const void* in, void* out,
         if (adjoint) sho_adjoint(s, din, dout, nbatch, st, nullptr);
         else sho_forward(s, din, dout, nbatch, st, nullptr);
         finish_out(s.st_out, adjoint ? bv : bm, st);
+    });
+}
+
+extern "C" int mmr_sho_set_tensor(mmr_sho* h, int on) {
+    return guarded([&] {
+        MMR_REQUIRE(h, "NULL argument");
+        reinterpret_cast<ShoPlan*>(h)->tensor = on != 0;
     });
 }
 

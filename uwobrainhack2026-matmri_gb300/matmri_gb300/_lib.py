@@ -114,6 +114,7 @@ SIGNATURES = {
     "mmr_sho_create": (C.c_int, [C.POINTER(ShoDesc), C.POINTER(C.c_void_p)]),
     "mmr_sho_apply": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
     "mmr_sho_destroy": (C.c_int, [C.c_void_p]),
+    "mmr_sho_set_tensor": (C.c_int, [C.c_void_p, C.c_int]),
     "mmr_sense_create": (C.c_int, [C.POINTER(SenseDesc), C.POINTER(C.c_void_p)]),
     "mmr_sense_apply": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mmr_sense_normal": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -7,8 +7,9 @@ the gridding kernels (``coil_group``), samples per gridding work item
 
 The search is a coordinate descent from the current setting: each knob in
 turn is swept over its candidates with the others fixed, for two rounds.
-Every candidate is timed with CUDA events around the normal operator
-(``mmr_sense_profile_normal``).  Results are cached per size class (image
+Every candidate is applied once untimed, then timed end to end with CUDA
+events around back-to-back normal operators (``mmr_sense_normal``), best of
+three.  Results are cached per size class (image
 size, oversampled grid, samples, coils, kernel width) and device in a JSON
 file (``$MATMRI_GB300_TUNE_CACHE`` or ``~/.cache/matmri_gb300/tuning.json``).
 """
@@ -54,13 +55,25 @@ def size_class(op) -> str:
     return f"N{'x'.join(map(str, op.imN))}_G{'x'.join(map(str, osN or []))}_M{op.M}_C{op.C}_W{kw}"
 
 
-def time_normal(op, x_ptr, y_ptr, reps=5) -> float:
-    """Mean ms of one normal operator application (sum over stages)."""
+def time_normal(op, x_ptr, y_ptr, reps=5, trials=3) -> float:
+    """ms of one normal operator application: CUDA events around `reps` back-to-back applications on
+    the current stream after one untimed application (which builds anything a setting needs first),
+    best of `trials`.  End to end, so per-kernel launch gaps count as they do in a solve."""
+    import torch
     lib = _lib.load()
-    ms = (C.c_double * 5)()
-    cnt = (C.c_int32 * 5)()
-    _lib.check(lib.mmr_sense_profile_normal(op.handle, x_ptr, y_ptr, int(reps), ms, cnt, None))
-    return sum(ms[i] for i in range(5)) / reps
+    st = torch.cuda.current_stream()
+    sp = st.cuda_stream
+    _lib.check(lib.mmr_sense_normal(op.handle, x_ptr, y_ptr, sp))
+    best = float("inf")
+    for _ in range(trials):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(reps):
+            _lib.check(lib.mmr_sense_normal(op.handle, x_ptr, y_ptr, sp))
+        e1.record(st)
+        e1.synchronize()
+        best = min(best, e0.elapsed_time(e1) / reps)
+    return best
 
 
 def autotune(op, reps=5, rounds=2, use_cache=True, verbose=False) -> dict:

@@ -248,6 +248,11 @@ class sampHighOrder(_Op):
         self._h = _Handle(h.value, lib.mmr_sho_destroy)
         self.V, self.M = V, M
 
+    def set_tensor(self, on: bool = True):
+        """Tensor-core contraction (default) or the SIMT FP32 kernels."""
+        _lib.check(_lib.load().mmr_sho_set_tensor(self.handle, int(bool(on))))
+        return self
+
     @property
     def handle(self):
         return self._h.ptr

@@ -16,9 +16,11 @@
 // and a low part scaled by 2^11 (the input columns first normalised to max 1),
 // and three products hi*hi + (hi*lo' + lo'*hi) / 2^11 are accumulated in FP32,
 // i.e. ~22-bit operands, FP32-level results (error vs FP64 in the tests).
-// Work split: a warp owns 32 output rows (two m16 tiles) x 8 NT columns; the
-// K range is split over gridDim.y CTAs whose partial sums a second kernel adds
-// in a fixed order.
+// Work split: a warp owns 16 TC_MTW output rows x 8 NT columns and loads the
+// phases of the next K step while it works on the current one; the K range is
+// split over gridDim.y CTAs whose partial sums a second kernel adds in a fixed
+// order.  The tensor-core accumulators are promoted into FP32 register sums
+// every TC_PROMOTE K steps.
 #include <algorithm>
 #include <cmath>
 
@@ -29,7 +31,8 @@
 namespace mmr {
 
 constexpr int TC_WARPS = 4;            // warps per CTA
-constexpr int TC_ROWS = 32 * TC_WARPS; // output rows per CTA
+constexpr int TC_MTW = 1;              // m16 tiles per warp (one keeps registers low, occupancy high)
+constexpr int TC_ROWS = 16 * TC_MTW * TC_WARPS; // output rows per CTA
 constexpr float TC_LO = 2048.f;        // scale of the low parts
 constexpr int TC_PROMOTE = 8;          // K steps (of 8 inputs) per tensor-core accumulation
 
@@ -119,43 +122,59 @@ __global__ void __launch_bounds__(TC_WARPS * 32) sho_tc_kernel(const float* __re
     if (active && *active) return;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int gid = lane >> 2, tig = lane & 3;
-    const long long row0 = (long long)blockIdx.x * TC_ROWS + warp * 32;
+    const long long row0 = (long long)blockIdx.x * TC_ROWS + warp * (16 * TC_MTW);
     const long long i0 = (long long)blockIdx.y * kchunk;             // first input element of this split
     const long long i1 = i0 + kchunk < L ? i0 + kchunk : L;
     // acc0 / acc1: the tensor-core accumulators of the current TC_PROMOTE K steps; tot: their sum,
     // added on the FP32 pipe, so that no tensor-core accumulation runs over more than
     // TC_PROMOTE x 16 products (its internal alignment of the addends costs accuracy as the
     // accumulator grows)
-    float acc0[2][NT][4], acc1[2][NT][4], tot[2][NT][4];
+    float acc0[TC_MTW][NT][4], acc1[TC_MTW][NT][4], tot[TC_MTW][NT][4];
 #pragma unroll
-    for (int m = 0; m < 2; ++m)
+    for (int m = 0; m < TC_MTW; ++m)
 #pragma unroll
         for (int n = 0; n < NT; ++n)
 #pragma unroll
             for (int j = 0; j < 4; ++j) acc0[m][n][j] = acc1[m][n][j] = tot[m][n][j] = 0.f;
     int steps = 0;
     // rows handled by this thread: row0 + 16 m + gid (+8)
-    long long rows[2][2];
+    long long rows[TC_MTW][2];
 #pragma unroll
-    for (int m = 0; m < 2; ++m) {
+    for (int m = 0; m < TC_MTW; ++m) {
         rows[m][0] = row0 + 16 * m + gid;
         rows[m][1] = rows[m][0] + 8;
     }
-    for (long long ib = i0; ib < i1; ib += 8) {
-        // A fragments: inputs ib + tig (k = 2 tig, 2 tig + 1) and ib + tig + 4 (k + 8)
-        uint32_t ah[2][4], al[2][4];
+    // phases of the next K step, loaded one step ahead to hide the table latency
+    auto load_turns = [&](long long ib, float (&t)[TC_MTW][4]) {
 #pragma unroll
-        for (int m = 0; m < 2; ++m) {
+        for (int m = 0; m < TC_MTW; ++m)
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
                 const long long rr = rows[m][q & 1];
                 const long long ii = ib + tig + (q >> 1) * 4;
-                float t = 0.f;
-                const bool ok = rr < R && ii < i1;
-                if (ok) t = ADJ ? turn[rr * M + ii] : turn[ii * M + rr];
+                t[m][q] = (rr < R && ii < i1) ? (ADJ ? turn[rr * M + ii] : turn[ii * M + rr]) : 0.f;
+            }
+    };
+    float tnext[TC_MTW][4];
+    load_turns(i0, tnext);
+    for (long long ib = i0; ib < i1; ib += 8) {
+        float tcur[TC_MTW][4];
+#pragma unroll
+        for (int m = 0; m < TC_MTW; ++m)
+#pragma unroll
+            for (int q = 0; q < 4; ++q) tcur[m][q] = tnext[m][q];
+        if (ib + 8 < i1) load_turns(ib + 8, tnext);
+        // A fragments: inputs ib + tig (k = 2 tig, 2 tig + 1) and ib + tig + 4 (k + 8)
+        uint32_t ah[TC_MTW][4], al[TC_MTW][4];
+#pragma unroll
+        for (int m = 0; m < TC_MTW; ++m) {
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const long long rr = rows[m][q & 1];
+                const long long ii = ib + tig + (q >> 1) * 4;
                 uint32_t h, l;
-                cs_split(t, h, l);
-                if (!ok) h = l = 0u;
+                cs_split(tcur[m][q], h, l);
+                if (!(rr < R && ii < i1)) h = l = 0u;
                 ah[m][q] = h;
                 al[m][q] = l;
             }
@@ -169,7 +188,7 @@ __global__ void __launch_bounds__(TC_WARPS * 32) sho_tc_kernel(const float* __re
             const uint32_t bl0 = *reinterpret_cast<const uint32_t*>(blo + boff);
             const uint32_t bl1 = *reinterpret_cast<const uint32_t*>(blo + boff + 8);
 #pragma unroll
-            for (int m = 0; m < 2; ++m) {
+            for (int m = 0; m < TC_MTW; ++m) {
                 mma16816(acc0[m][n], ah[m][0], ah[m][1], ah[m][2], ah[m][3], bh0, bh1);
                 mma16816(acc1[m][n], ah[m][0], ah[m][1], ah[m][2], ah[m][3], bl0, bl1);
                 mma16816(acc1[m][n], al[m][0], al[m][1], al[m][2], al[m][3], bh0, bh1);
@@ -178,7 +197,7 @@ __global__ void __launch_bounds__(TC_WARPS * 32) sho_tc_kernel(const float* __re
         if (++steps == TC_PROMOTE || ib + 8 >= i1) {
             steps = 0;
 #pragma unroll
-            for (int m = 0; m < 2; ++m)
+            for (int m = 0; m < TC_MTW; ++m)
 #pragma unroll
                 for (int n = 0; n < NT; ++n)
 #pragma unroll
@@ -190,7 +209,7 @@ __global__ void __launch_bounds__(TC_WARPS * 32) sho_tc_kernel(const float* __re
     }
     float* out = partial + (long long)blockIdx.y * R * (8 * NT);
 #pragma unroll
-    for (int m = 0; m < 2; ++m)
+    for (int m = 0; m < TC_MTW; ++m)
 #pragma unroll
         for (int h = 0; h < 2; ++h) {
             const long long rr = rows[m][h];

@@ -523,22 +523,32 @@ __global__ void __launch_bounds__(256) interp2d_binned(const float2* __restrict_
 // Two cells per thread-iteration (float4); T is a power of two, te1 is even.
 // Owned (sub)tiles are written with plain float4 stores; a leaf tile shared by
 // several items (pre-zeroed) receives vector reductions of its non-zero cells.
-__device__ __forceinline__ void flush_tile(const float2* acc, float2* __restrict__ out, bool shared, int T, int u0,
+// Spreading accumulators in shared memory: per coil a real and an imaginary plane of
+// T rows x (T + 4) floats (all real planes, then all imaginary planes), plane stride
+// (T + 4) T + 16 floats.  Row stride = 4 (mod 32) words and adjacent coils' planes 16
+// (mod 32) words apart put the 16 taps of a 4 x 4 footprint of two coils (one warp's
+// atomics) on 32 distinct banks; a float2 tile with separate .x / .y atomics put four
+// rows on the same banks.
+__device__ __forceinline__ int acc_row(int T) { return T + 4; }
+__device__ __forceinline__ int acc_plane(int T) { return (T + 4) * T + 16; }
+inline size_t acc_plane_host(int T) { return (size_t)(T + 4) * T + 16; }
+
+__device__ __forceinline__ void flush_tile(const float* acc, float2* __restrict__ out, bool shared, int T, int u0,
                                            int v0, int te1, int te2, int c0, const Bin2DArgs& a) {
     const int lgT = 31 - __clz(T);
-    const int n2 = (a.cg << (2 * lgT)) >> 1;
-    const float4* acc4 = reinterpret_cast<const float4*>(acc);
-    for (int h = threadIdx.x; h < n2; h += blockDim.x) {
-        const int i = h << 1;
+    const int PS = acc_plane(T), RS = acc_row(T);
+    const float* im = acc + (size_t)a.cg * PS;
+    const int n = a.cg << (2 * lgT);
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
         const int c = i >> (2 * lgT), r = i & ((1 << (2 * lgT)) - 1), l2 = r >> lgT, l1 = r & (T - 1);
         if (l1 < te1 && l2 < te2 && c0 + c < a.nb) {
             float2* d = out + (u0 + l1) + (long long)a.G1 * ((v0 + l2) + (long long)a.G2 * (c0 + c));
-            const float4 v = acc4[h];
+            const int k = c * PS + l2 * RS + l1;
+            const float2 v = make_float2(acc[k], im[k]);
             if (!shared) {
-                *reinterpret_cast<float4*>(d) = v;
-            } else {
-                if (v.x != 0.f || v.y != 0.f) atomicAdd(d, make_float2(v.x, v.y));
-                if (v.z != 0.f || v.w != 0.f) atomicAdd(d + 1, make_float2(v.z, v.w));
+                *d = v;
+            } else if (v.x != 0.f || v.y != 0.f) {
+                atomicAdd(d, v);
             }
         }
     }
@@ -565,9 +575,10 @@ static void zero_shared(NufftPlan& p, float2* out, long long nb, cudaStream_t st
     check_launch("zero_shared_tiles");
 }
 
-__device__ __forceinline__ void zero_acc(float2* acc, int n) {
+// Zeroes n floats (n a multiple of 4).
+__device__ __forceinline__ void zero_acc(float* acc, int n) {
     float4* a4 = reinterpret_cast<float4*>(acc);
-    for (int h = threadIdx.x; h < (n >> 1); h += blockDim.x) a4[h] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int h = threadIdx.x; h < (n >> 2); h += blockDim.x) a4[h] = make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
 template <int W>
@@ -576,14 +587,15 @@ __global__ void __launch_bounds__(256) spread2d_binned(const float2* __restrict_
     using TM = TapMap<W>;
     extern __shared__ float4 sm4[];
     if (a.active && *a.active) return;
-    float2* acc = reinterpret_cast<float2*>(sm4);
+    float* acc = reinterpret_cast<float*>(sm4);
     const int4 item = a.items[blockIdx.x];
     const int T = item.w & 255;                // this item's (sub)tile side
     const bool shared = (item.w >> 8) != 0;    // tile split across several items
     const int u0 = item.x & 0xffff, v0 = item.x >> 16;
     const int c0 = blockIdx.y * a.cg;
     const int te1 = min(T, a.G1 - u0), te2 = min(T, a.G2 - v0);
-    zero_acc(acc, a.cg * T * T);
+    const int PS = acc_plane(T), RS = acc_row(T);
+    zero_acc(acc, 2 * a.cg * PS);
     __syncthreads();
     const int e0 = item.y, e1 = item.z;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
@@ -602,7 +614,7 @@ __global__ void __launch_bounds__(256) spread2d_binned(const float2* __restrict_
             const int l1 = lb.x + off0 + ta, l2 = lb.y + off0 + tb;
             const bool ok = k < TM::TAPS && l1 >= 0 && l1 < te1 && l2 >= 0 && l2 < te2;
             wt[i] = ok ? w[ta] * w[W + tb] : 0.f;
-            ao[i] = ok ? l2 * T + l1 : -1;
+            ao[i] = ok ? l2 * RS + l1 : -1;
         }
         for (int cb = 0; cb < a.cg; cb += TM::PPW) {
             const int c = cb + grp;
@@ -613,12 +625,13 @@ __global__ void __launch_bounds__(256) spread2d_binned(const float2* __restrict_
                 v.x *= f;
                 v.y *= f;
             }
-            float2* ac = acc + (size_t)c * T * T;
+            float* re = acc + (size_t)c * PS;
+            float* im = re + (size_t)a.cg * PS;
 #pragma unroll
             for (int i = 0; i < TM::TPL; ++i) {
                 if (ao[i] >= 0) {
-                    atomicAdd(&ac[ao[i]].x, wt[i] * v.x);
-                    atomicAdd(&ac[ao[i]].y, wt[i] * v.y);
+                    atomicAdd(re + ao[i], wt[i] * v.x);
+                    atomicAdd(im + ao[i], wt[i] * v.y);
                 }
             }
         }
@@ -636,14 +649,15 @@ __global__ void __launch_bounds__(256) gridnorm2d_binned(const float2* __restric
     const int R0 = a.T + 2 * W;                // region side of a full tile (smem layout)
     uint64_t* bar;
     float2* reg = tma_layout(sm4, &bar);
-    float2* acc = reg + (size_t)a.cg * R0 * R0;
+    float* acc = reinterpret_cast<float*>(reg + (size_t)a.cg * R0 * R0);
     const int4 item = a.items[blockIdx.x];
     const int T = item.w & 255, R = T + 2 * W; // this item's (sub)tile and region sides
     const bool shared = (item.w >> 8) != 0;    // tile split across several items
     const int u0 = item.x & 0xffff, v0 = item.x >> 16;
     const int c0 = blockIdx.y * a.cg;
     const int te1 = min(T, a.G1 - u0), te2 = min(T, a.G2 - v0);
-    zero_acc(acc, a.cg * T * T);
+    const int PS = acc_plane(T), RS = acc_row(T);
+    zero_acc(acc, 2 * a.cg * PS);
     const int e0 = item.y, e1 = item.z;
     mbar_init(bar);
     if (e1 > e0) {
@@ -655,7 +669,8 @@ __global__ void __launch_bounds__(256) gridnorm2d_binned(const float2* __restric
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
     constexpr int off0 = -W / 2 + 1;
-    float2* sval = acc + (size_t)a.cg * a.T * a.T;      // interpolated, weighted samples [entry][coil]
+    // interpolated, weighted samples [entry][coil], after the accumulators of a full tile
+    float2* sval = reinterpret_cast<float2*>(acc + (size_t)2 * a.cg * acc_plane(a.T));
     int lgcg = 0;
     while ((1 << lgcg) < a.cg) ++lgcg;
     // entries are processed in batches of a.chunk (the capacity of sval)
@@ -709,19 +724,20 @@ __global__ void __launch_bounds__(256) gridnorm2d_binned(const float2* __restric
             const int l1 = lb.x + off0 + ta, l2 = lb.y + off0 + tb;
             const bool ok = k < TM::TAPS && l1 >= 0 && l1 < te1 && l2 >= 0 && l2 < te2;
             wt[i] = ok ? w[ta] * w[W + tb] : 0.f;
-            ao[i] = ok ? l2 * T + l1 : -1;
+            ao[i] = ok ? l2 * RS + l1 : -1;
         }
         const float2* sv = sval + ((e - eb) << lgcg);
         for (int cb = 0; cb < a.cg; cb += TM::PPW) {
             const int c = cb + grp;
             if (c >= a.cg || c0 + c >= a.nb) continue;
             const float2 v = sv[c];
-            float2* ac = acc + (size_t)c * T * T;
+            float* re = acc + (size_t)c * PS;
+            float* im = re + (size_t)a.cg * PS;
 #pragma unroll
             for (int i = 0; i < TM::TPL; ++i) {
                 if (ao[i] >= 0) {
-                    atomicAdd(&ac[ao[i]].x, wt[i] * v.x);
-                    atomicAdd(&ac[ao[i]].y, wt[i] * v.y);
+                    atomicAdd(re + ao[i], wt[i] * v.x);
+                    atomicAdd(im + ao[i], wt[i] * v.y);
                 }
             }
         }
@@ -924,8 +940,8 @@ void nufft_spread(NufftPlan& p, const float2* y, float2* grid, long long nb, con
         return;
     }
     const int T = p.bins.T;
-    const int cg = pick_cg(p, nb, (size_t)T * T * 8, 0);
-    const size_t smem = (size_t)cg * T * T * 8;
+    const int cg = pick_cg(p, nb, acc_plane_host(T) * 8, 0);
+    const size_t smem = (size_t)cg * acc_plane_host(T) * 8;
     Bin2DArgs a = bin_args(p, false, wfac, wfb, nb, cg, false, active);
     dim3 gridDim((unsigned)p.bins.n_pad_items, (unsigned)cdiv(nb, cg));
     zero_shared(p, grid, nb, st, active);
@@ -944,7 +960,7 @@ void nufft_grid_normal(NufftPlan& p, const float2* gin, float2* gout, long long 
                        cudaStream_t st, const int* active) {
     MMR_REQUIRE(p.use_bins, "fused gridding needs the 2D binned path");
     const int T = p.bins.T, R = T + 2 * p.W;
-    const int cg = pick_cg(p, nb, (size_t)(R * R + T * T + p.bins.chunk) * 8, kTmaSmemExtra);
+    const int cg = pick_cg(p, nb, ((size_t)R * R + acc_plane_host(T) + p.bins.chunk) * 8, kTmaSmemExtra);
     static const void* cptr = nullptr;
     static long long cnb = 0;
     static int ccg = 0, cR = 0, cG1 = 0, cG2 = 0;
@@ -957,7 +973,7 @@ void nufft_grid_normal(NufftPlan& p, const float2* gin, float2* gout, long long 
         cG1 = p.G[0];
         cG2 = p.G[1];
     }
-    const size_t smem = kTmaSmemExtra + (size_t)cg * (R * R + T * T + p.bins.chunk) * 8;
+    const size_t smem = kTmaSmemExtra + (size_t)cg * ((size_t)R * R + acc_plane_host(T) + p.bins.chunk) * 8;
     Bin2DArgs a = bin_args(p, false, wfac, wfb, nb, cg, true, active);
     dim3 gridDim((unsigned)p.bins.n_pad_items, (unsigned)cdiv(nb, cg));
     zero_shared(p, gout, nb, st, active);

@@ -99,13 +99,14 @@ __global__ void lp_init_kernel(const float2* __restrict__ b, const float2* __res
     double* const dst[2] = {&st->rr, &st->mse};
     block_accumulate<2>(v, dst);
     if (last_block_of(&st->counter)) {
-        volatile LpState* vs = st;
         if (!judge) {
-            vs->rr0 = vs->rr;
-            hist[0] = vs->rr;
-            hist[vs->cap] = vs->mse;
+            const double rr = __ldcg(&st->rr), mse = __ldcg(&st->mse);
+            st->rr0 = rr;
+            hist[0] = rr;
+            hist[st->cap] = mse;
         }
-        vs->counter = 0;
+        st->counter = 0;
+        __threadfence();
     }
 }
 
@@ -166,36 +167,38 @@ __global__ void lp_update_kernel(float2* __restrict__ x, const float2* __restric
     double* const dst[2] = {&st->rr, &st->mse};
     block_accumulate<2>(v, dst);
     if (last_block_of(&st->counter)) {
-        volatile LpState* vs = st;
-        const int k = vs->nit + 1;
-        const double rr = vs->rr;
-        const int cap = vs->cap;
-        vs->pqh[2 * vs->slot] = bad ? 0.0 : pqr;
-        vs->pqh[2 * vs->slot + 1] = bad ? 0.0 : pqi;
+        LpState s;
+        state_copy_in(s, st);
+        const int k = s.nit + 1;
+        const double rr = s.rr;
+        const int cap = s.cap;
+        s.pqh[2 * s.slot] = bad ? 0.0 : pqr;
+        s.pqh[2 * s.slot + 1] = bad ? 0.0 : pqi;
         if (k < cap) {
             hist[k] = rr;
-            hist[cap + k] = vs->mse;
+            hist[cap + k] = s.mse;
         }
         // a stall counts only above the precision floor of complex64 vectors (|r| ~ 1e-6 |r0|),
         // where any residual stops falling
-        if (vs->window > 0 && !vs->plain && k >= vs->window && k - vs->window < cap && rr >= hist[k - vs->window] &&
-            rr > LP_FLOOR * vs->rr0)
-            vs->stalled = 1;
-        if (bad && !vs->plain) vs->stalled = 1;
-        if (vs->stalled && !vs->plain) {   // fall back to plain CG from this x
-            vs->plain = 1;
-            vs->restart = 1;
-            vs->fell_at = k;
+        if (s.window > 0 && !s.plain && k >= s.window && k - s.window < cap && rr >= __ldcg(hist + k - s.window) &&
+            rr > LP_FLOOR * s.rr0)
+            s.stalled = 1;
+        if (bad && !s.plain) s.stalled = 1;
+        if (s.stalled && !s.plain) {   // fall back to plain CG from this x
+            s.plain = 1;
+            s.restart = 1;
+            s.fell_at = k;
         }
         int fin = 0;
-        if (vs->tol2 > 0 && rr <= vs->tol2 * vs->rr0) {
+        if (s.tol2 > 0 && rr <= s.tol2 * s.rr0) {
             fin = 1;
-            vs->status = 1;
+            s.status = 1;
         }
-        if (k >= vs->nitmax) fin = 1;
-        vs->nit = k;
-        if (fin) vs->finished = 1;
-        vs->counter = 0;
+        if (k >= s.nitmax) fin = 1;
+        s.nit = k;
+        if (fin) s.finished = 1;
+        s.counter = 0;
+        state_copy_out(st, s);
     }
 }
 
@@ -227,24 +230,27 @@ __global__ void lp_qz_kernel(const float2* __restrict__ ring_q, const float2* __
     for (int j = 0; j < 2 * LP_MAXM; ++j) dst[j] = j < 2 * nv ? &st->qz[j] : nullptr;
     block_accumulate<2 * LP_MAXM>(v, dst);
     if (last_block_of(&st->counter2)) {
-        volatile LpState* vs = st;
-        const bool restart = vs->restart;
+        LpState s;
+        state_copy_in(s, st);
+        const bool restart = s.restart;
+#pragma unroll
         for (int j = 0; j < LP_MAXM; ++j) {
             double2 bt = make_double2(0.0, 0.0);
-            const double pr = vs->pqh[2 * j], pi = vs->pqh[2 * j + 1];
-            if (!restart && j < nv && pr * pr + pi * pi > 0.0)
-                bt = cdiv_d(-vs->qz[2 * j], -vs->qz[2 * j + 1], pr, pi);
+            const double pr = s.pqh[2 * j], pi = s.pqh[2 * j + 1];
+            if (!restart && j < nv && pr * pr + pi * pi > 0.0) bt = cdiv_d(-s.qz[2 * j], -s.qz[2 * j + 1], pr, pi);
             if (!isfinite(bt.x + bt.y)) bt = make_double2(0.0, 0.0);
-            vs->beta[2 * j] = bt.x;
-            vs->beta[2 * j + 1] = bt.y;
+            s.beta[2 * j] = bt.x;
+            s.beta[2 * j + 1] = bt.y;
         }
         // valid ring entries are always slots [0, nstored): a restart begins again at slot 0
-        vs->nstored = restart ? 0 : nv;
-        vs->restart = 0;
-        vs->slot = restart ? 0 : (vs->slot + 1) % m;
-        vs->pq_re = vs->pq_im = vs->pr_re = vs->pr_im = vs->rr = vs->mse = 0.0;
-        for (int j = 0; j < 2 * LP_MAXM; ++j) vs->qz[j] = 0.0;
-        vs->counter2 = 0;
+        s.nstored = restart ? 0 : nv;
+        s.restart = 0;
+        s.slot = restart ? 0 : (s.slot + 1) % m;
+        s.pq_re = s.pq_im = s.pr_re = s.pr_im = s.rr = s.mse = 0.0;
+#pragma unroll
+        for (int j = 0; j < 2 * LP_MAXM; ++j) s.qz[j] = 0.0;
+        s.counter2 = 0;
+        state_copy_out(st, s);
     }
 }
 

@@ -49,4 +49,25 @@ __device__ __forceinline__ bool last_block_of(unsigned int* counter) {
     return false;
 }
 
+// Copies a device state struct (a whole number of 8-byte words, updated by other
+// blocks' atomics) into registers with independent L2 loads, and back.  For the
+// one thread that finalises an iteration: one round trip instead of one per field.
+template <class S>
+__device__ __forceinline__ void state_copy_in(S& s, const S* g) {
+    static_assert(sizeof(S) % 8 == 0, "state must be a whole number of 8-byte words");
+    const unsigned long long* src = reinterpret_cast<const unsigned long long*>(g);
+    unsigned long long* dst = reinterpret_cast<unsigned long long*>(&s);
+#pragma unroll
+    for (int i = 0; i < (int)(sizeof(S) / 8); ++i) dst[i] = __ldcg(src + i);
+}
+
+template <class S>
+__device__ __forceinline__ void state_copy_out(S* g, const S& s) {
+    unsigned long long* dst = reinterpret_cast<unsigned long long*>(g);
+    const unsigned long long* src = reinterpret_cast<const unsigned long long*>(&s);
+#pragma unroll
+    for (int i = 0; i < (int)(sizeof(S) / 8); ++i) __stcg(dst + i, src[i]);
+    __threadfence();
+}
+
 }  // namespace mmr

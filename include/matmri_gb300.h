@@ -152,6 +152,28 @@ MMR_API int mmr_sho_apply(mmr_sho* s, int adjoint, const void* in, void* out,
 MMR_API int mmr_sho_set_tensor(mmr_sho* s, int on);
 MMR_API int mmr_sho_destroy(mmr_sho* s);
 
+/* Replaces sampHighOrder(..., approach = 1, opt): the SVD + NUFFT
+ * interpolated encoding (useInterpWorker, sampHighOrder.m:314-359).  The
+ * caller passes the factors that prepForInterp forms (sampHighOrder.m:700-889,
+ * createNufftForInterp 624-698): kloc [M x 2] of the trajectory nufftOp,
+ * svd_space [V x L], svd_time [M x L] and phs_shift [M], all host doubles,
+ * the last three interleaved complex.  os / kwidth of the trajectory nufftOp
+ * (<= 0: the nufftOp defaults 1.5 / 6).  2D images only.  The handle works
+ * with mmr_sho_apply and mmr_sense_create like the direct encoding.        */
+typedef struct mmr_sho_interp_desc {
+    int32_t       ndim;        /* 2                                           */
+    int64_t       imN[3];
+    int64_t       nsamp;       /* M                                           */
+    int32_t       nterms;      /* L (number of singular triplets kept)        */
+    const double* kloc;
+    const double* svd_space;
+    const double* svd_time;
+    const double* phs_shift;
+    double        os;
+    int32_t       kwidth;
+} mmr_sho_interp_desc;
+MMR_API int mmr_sho_interp_create(const mmr_sho_interp_desc* desc, mmr_sho** out);
+
 /* ---- mrSampFunc --------------------------------------------------------------
  * Replaces opFunc = @(x,transp) mrSampFunc(x, transp, S, R, opt)
  *   (operators/mrSampFunc.m:1-160) for S a nufftOp or sampHighOrder and R an

@@ -98,7 +98,7 @@ class ShoRef:
         ps = np.asarray(phs_spha, dtype=np.float64)
         self.phs_spha = ps.reshape(ps.shape[0], -1, order="F")
         pc = np.asarray(phs_conc, dtype=np.float64) if phs_conc is not None and np.size(phs_conc) else np.zeros((0, self.M))
-        self.phs_conc = pc.reshape(pc.shape[0], -1, order="F")
+        self.phs_conc = pc.reshape(pc.shape[0], self.M, order="F")
         self.b0mask = None if b0mask is None or np.size(b0mask) == 0 else \
             np.asarray(b0mask, dtype=np.float64).reshape(-1, order="F")
         self.adjoint = False

@@ -107,3 +107,69 @@ def test_tensor_core_contraction(mm, ncoil, shape):
     S.set_tensor(False)
     assert rel(yt, S * x) < 1e-5
     assert rel(xt, S.H * y) < 1e-5
+
+
+# ---- approach 1: SVD + NUFFT interpolated encoding (sampHighOrder.m:314-359) ----
+def _interp_op(mm, case, grid, mask=None):
+    return mm.sampHighOrder(case["b0"], case["t"], case["spha"], case["coco"], grid, mask, 1, 0, 1,
+                            {"svdThresh": 0.01, "subFact": 5})
+
+
+@pytest.mark.parametrize("orient", [0, 1, 2, 3])
+def test_interp_vs_restatement_same_factors(mm, orient):
+    # the device applies the host-formed factors: forward / adjoint against the FP64 useInterpWorker
+    from oracle.sho_interp_ref import ShoInterpRef
+    from sho_cases import interp_case, orient_grid
+    case = interp_case(32, seed=1)
+    grid = orient_grid(case, orient)
+    S = _interp_op(mm, case, grid)
+    f = dict(kloc=S.traj_kloc, phsShft=S.phsShft, svdTime=S.svdTime, svdSpace=S.svdSpace)
+    R = ShoInterpRef([32, 32], f)
+    rng = np.random.default_rng(orient)
+    x = crandn(rng, (32, 32, 3))
+    y = crandn(rng, (case["M"], 3))
+    assert rel(S * x, R.mtimes(x)) < 1e-5
+    assert rel(S.H * y, R.H.mtimes(y)) < 1e-5
+
+
+@pytest.mark.parametrize("orient", [0, 2])
+def test_interp_reference_criteria(mm, orient):
+    # tests.m:127-139 (useSingle branch 149-155: adjoint to 1e-5) and the comparison with the direct encoding
+    from sho_cases import interp_case, orient_grid
+    case = interp_case(64, seed=1)
+    grid = orient_grid(case, orient)
+    S = _interp_op(mm, case, grid)
+    rng = np.random.default_rng(5)
+    x = crandn(rng, (64, 64))
+    y = crandn(rng, case["M"])
+    Sx, Sy = S * x, S.H * y
+    d1 = np.vdot(x.ravel(order="F"), Sy.ravel(order="F"))
+    d2 = np.vdot(Sx.ravel(), y)
+    assert abs(d1 - d2) / min(abs(d1), abs(d2)) < 1e-5
+    direct = ShoRef(case["b0"], case["t"], case["spha"], case["coco"], grid).mtimes(x).ravel()
+    assert np.linalg.norm(direct - Sx.ravel()) / direct.size < 1e-4
+
+
+def test_interp_masked_and_sense_cgne(mm):
+    # a b0 mask (sampHighOrder.m:808-818, 854-858) and the encoding inside mrSampFunc + cgne with coils
+    from oracle.sense_ref import RcvrRef, cgne_ref, mrsampfunc
+    from oracle.sho_interp_ref import ShoInterpRef
+    from sho_cases import interp_case, orient_grid
+    from matmri_gb300 import synth
+    case = interp_case(32, seed=4)
+    grid = orient_grid(case, 1)
+    mask = (case["x"] ** 2 + case["y"] ** 2) < (0.9 * np.abs(case["x"]).max()) ** 2
+    S = _interp_op(mm, case, grid, mask)
+    assert np.all(S.svdSpace[~mask.reshape(-1, order="F")] == 0)
+    f = dict(kloc=S.traj_kloc, phsShft=S.phsShft, svdTime=S.svdTime, svdSpace=S.svdSpace)
+    Sr = ShoInterpRef([32, 32], f)
+    maps = synth.coil_maps(32, 4, 1)
+    A = mm.mrSampOp(S, mm.rcvrOp(maps, 0))
+    Rr = RcvrRef(maps)
+    img = synth.ellipse_phantom(32, 6, 2, complex_phase=True)
+    data = mrsampfunc(img, "notransp", Sr, Rr)
+    assert rel(A(img, "notransp"), data) < 1e-5
+    opt = {"xChangeThresh": None, "resThresh": None}
+    x, *_ = mm.cgne(A, data, None, 6, opt)
+    xr, *_ = cgne_ref(lambda v, tr: mrsampfunc(v, tr, Sr, Rr), data, None, 6, opt)
+    assert rel(x, xr) < 1e-4

@@ -17,6 +17,7 @@
 #include <cmath>
 
 #include "sense.cuh"
+#include "sho_interp.cuh"
 #include "sho_tc.cuh"
 
 namespace mmr {
@@ -32,6 +33,7 @@ struct ShoPlan {
     bool table = false;
     bool tensor = true;     // with the table: tensor-core contraction (sho_tc.cu), else the SIMT kernels
     ShoTcScratch tc;
+    std::shared_ptr<ShoInterp> interp;   // approach 1 (sho_interp.cu); the fields above stay empty
     Staged st_in, st_out;
 };
 
@@ -210,6 +212,10 @@ __global__ void __launch_bounds__(256) sho_adj_kernel(const float* __restrict__ 
 }
 
 void sho_forward(ShoPlan& s, const float2* x, float2* y, long long nb, cudaStream_t st, const int* active) {
+    if (s.interp) {
+        sho_interp_forward(*s.interp, x, y, nb, st, active);
+        return;
+    }
     if (s.table && s.tensor && nb <= SHO_TC_MAX_COILS) {
         sho_tc_forward(s.tc, s.d_turn.as<float>(), s.V, s.M, x, y, nb, st, active);
         return;
@@ -231,6 +237,10 @@ void sho_forward(ShoPlan& s, const float2* x, float2* y, long long nb, cudaStrea
 }
 
 void sho_adjoint(ShoPlan& s, const float2* y, float2* x, long long nb, cudaStream_t st, const int* active) {
+    if (s.interp) {
+        sho_interp_adjoint(*s.interp, y, x, nb, st, active);
+        return;
+    }
     if (s.table && s.tensor && nb <= SHO_TC_MAX_COILS) {
         sho_tc_adjoint(s.tc, s.d_turn.as<float>(), s.V, s.M, y, x, nb, st, active);
         return;
@@ -333,6 +343,27 @@ extern "C" int mmr_sho_create(const mmr_sho_desc* desc, mmr_sho** out) {
     });
 }
 
+extern "C" int mmr_sho_interp_create(const mmr_sho_interp_desc* desc, mmr_sho** out) {
+    return guarded([&] {
+        MMR_REQUIRE(desc && out, "NULL argument");
+        *out = nullptr;
+        auto* s = new ShoPlan();
+        try {
+            s->interp = sho_interp_build(*desc);
+            s->nd = 2;
+            s->imN[0] = desc->imN[0];
+            s->imN[1] = desc->imN[1];
+            s->V = sho_interp_nvox(*s->interp);
+            s->M = sho_interp_nsamp(*s->interp);
+            s->tensor = false;
+        } catch (...) {
+            delete s;
+            throw;
+        }
+        *out = reinterpret_cast<mmr_sho*>(s);
+    });
+}
+
 extern "C" int mmr_sho_apply(mmr_sho* h, int adjoint, const void* in, void* out, int64_t nbatch, void* stream) {
     return guarded([&] {
         MMR_REQUIRE(h && in && out && nbatch >= 1, "bad argument");
@@ -344,6 +375,8 @@ extern "C" int mmr_sho_apply(mmr_sho* h, int adjoint, const void* in, void* out,
         if (adjoint) sho_adjoint(s, din, dout, nbatch, st, nullptr);
         else sho_forward(s, din, dout, nbatch, st, nullptr);
         finish_out(s.st_out, adjoint ? bv : bm, st);
+        if (s.interp && s.st_out.host && device_error_word(st))
+            MMR_THROW(MMR_ERR_TIMEOUT, "a bounded device wait ran out");
     });
 }
 

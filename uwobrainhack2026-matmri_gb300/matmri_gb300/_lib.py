@@ -38,6 +38,13 @@ class ShoDesc(C.Structure):
                 ("gz", C.POINTER(C.c_double)), ("mask", C.POINTER(C.c_double))]
 
 
+class ShoInterpDesc(C.Structure):
+    _fields_ = [("ndim", C.c_int32), ("imN", C.c_int64 * 3), ("nsamp", C.c_int64), ("nterms", C.c_int32),
+                ("kloc", C.POINTER(C.c_double)), ("svd_space", C.POINTER(C.c_double)),
+                ("svd_time", C.POINTER(C.c_double)), ("phs_shift", C.POINTER(C.c_double)),
+                ("os", C.c_double), ("kwidth", C.c_int32)]
+
+
 class SenseDesc(C.Structure):
     _fields_ = [("nufft", C.c_void_p), ("sho", C.c_void_p), ("rcvr", C.c_void_p),
                 ("W", C.POINTER(C.c_float)), ("w_per_coil", C.c_int32), ("tikreg", C.c_double)]
@@ -115,6 +122,7 @@ SIGNATURES = {
     "mmr_sho_apply": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
     "mmr_sho_destroy": (C.c_int, [C.c_void_p]),
     "mmr_sho_set_tensor": (C.c_int, [C.c_void_p, C.c_int]),
+    "mmr_sho_interp_create": (C.c_int, [C.POINTER(ShoInterpDesc), C.POINTER(C.c_void_p)]),
     "mmr_sense_create": (C.c_int, [C.POINTER(SenseDesc), C.POINTER(C.c_void_p)]),
     "mmr_sense_apply": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p]),
     "mmr_sense_normal": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]),

@@ -199,8 +199,13 @@ class sampHighOrder(_Op):
     """S = sampHighOrder(b0, sampTimes, phs_spha, phs_conc, phs_grid, imMask, useGPU, useSingle, approach, opt).
 
     Approaches 0, 2 and 3 compute the same sums (direct / segmented) and map
-    to the same device kernels; approach 1 (SVD + NUFFT interpolation,
-    sampHighOrder.m:314-359) is not in this build.
+    to the same device kernels.  Approach 1 is the SVD + NUFFT interpolated
+    encoding (sampHighOrder.m:314-359, prepForInterp 700-889): the factors
+    are formed on the host (``sho_interp.prep_for_interp``; opt.svdThresh,
+    opt.subFact, opt.svdNtry) and applied on the device; opt.subFactSpc > 1
+    and SMS slice stacks are not supported (ValueError).  The factors stay
+    readable as ``svdSpace``, ``svdTime``, ``phsShft`` and the trajectory
+    ``traj_kloc``.
     """
 
     def __init__(self, b0=None, sampTimes=None, phs_spha=None, phs_conc=None, phs_grid=None, b0mask=None,
@@ -209,7 +214,8 @@ class sampHighOrder(_Op):
             raise TypeError("sampHighOrder() with no arguments runs the reference self-tests; use pytest tests/")
         self.approach = 0 if approach is None else int(approach)
         if self.approach == 1:
-            raise NotImplementedError("sampHighOrder approach 1 (interpolated) is not in this build")
+            self._init_interp(b0, sampTimes, phs_spha, phs_conc, phs_grid, b0mask, opt or {})
+            return
         lib = _lib.load()
         gx = np.asarray(phs_grid["x"], dtype=np.float64)
         self.imSize = list(gx.shape) if not (gx.ndim == 2 and gx.shape[1] == 1) else [gx.shape[0]]
@@ -247,6 +253,45 @@ class sampHighOrder(_Op):
         _lib.check(lib.mmr_sho_create(C.byref(d), C.byref(h)))
         self._h = _Handle(h.value, lib.mmr_sho_destroy)
         self.V, self.M = V, M
+
+    def _init_interp(self, b0, sampTimes, phs_spha, phs_conc, phs_grid, b0mask, opt):
+        from .sho_interp import prep_for_interp
+        opt = dict(opt)
+        if opt.get("subFactSpc") not in (None, 1):
+            raise ValueError("opt.subFactSpc > 1 is not supported by the interpolated approach here")
+        lib = _lib.load()
+        gx = np.asarray(phs_grid["x"], dtype=np.float64)
+        if gx.ndim != 2:
+            raise ValueError("the interpolated approach is built for 2-D grids (no SMS slice stacks)")
+        t = np.asarray(sampTimes, dtype=np.float64)
+        self.imSize = list(gx.shape)
+        self.kSize = list(t.shape) if not (t.ndim == 2 and t.shape[1] == 1) else [t.shape[0]]
+        if b0 is not None and np.size(b0) and np.size(b0) != gx.size:
+            raise ValueError("Size mismatch between b0 and phs_grid.x")                # sampHighOrder.m:223-224
+        self.svdThresh = 0.05 if opt.get("svdThresh") is None else float(opt["svdThresh"])
+        self.subFact = 5 if opt.get("subFact") is None else max(1, int(opt["subFact"]))
+        f = prep_for_interp(b0, t, phs_spha, phs_conc, phs_grid, b0mask, self.svdThresh, self.subFact,
+                            opt.get("svdNtry"))
+        self.svdSpace, self.svdTime, self.phsShft, self.traj_kloc = f["svdSpace"], f["svdTime"], f["phsShft"], \
+            f["kloc"]
+        L = f["s"].size
+        k = dict(kloc=np.asfortranarray(f["kloc"]),
+                 space=np.asfortranarray(f["svdSpace"], dtype=np.complex128),
+                 time=np.asfortranarray(f["svdTime"], dtype=np.complex128),
+                 shift=np.ascontiguousarray(f["phsShft"], dtype=np.complex128))
+        self._keep = k
+        d = _lib.ShoInterpDesc()
+        d.ndim = 2
+        d.imN[0], d.imN[1], d.imN[2] = self.imSize[0], self.imSize[1], 1
+        d.nsamp = t.size
+        d.nterms = L
+        cp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))
+        d.kloc, d.svd_space, d.svd_time, d.phs_shift = cp(k["kloc"]), cp(k["space"]), cp(k["time"]), cp(k["shift"])
+        d.os, d.kwidth = 0.0, 0
+        h = C.c_void_p()
+        _lib.check(lib.mmr_sho_interp_create(C.byref(d), C.byref(h)))
+        self._h = _Handle(h.value, lib.mmr_sho_destroy)
+        self.V, self.M = gx.size, t.size
 
     def set_tensor(self, on: bool = True):
         """Tensor-core contraction (default) or the SIMT FP32 kernels."""

@@ -151,6 +151,15 @@ MMR_API int mmr_sho_apply(mmr_sho* s, int adjoint, const void* in, void* out,
  * for the table the SIMT kernels evaluate the phase per element in FP64.  */
 MMR_API int mmr_sho_set_tensor(mmr_sho* s, int on);
 MMR_API int mmr_sho_destroy(mmr_sho* s);
+/* Replaces S2 = S.setPhiDiv(ksphaDiv, kconcDiv) (sampHighOrder.m:590-622):
+ * a new handle whose forward is (1i * exp(1i*kbase) .* phiDiv).' * x / sqrt(V)
+ * with phiDiv from prepForDirect on the derivative coefficients (no B0 term;
+ * sampHighOrder.m:376-380) and whose adjoint is the base's (369-372).
+ * kspha_div [nspha x M], kconc_div [nconc x M] host doubles, nspha / nconc at
+ * most the base plan's.  The new handle refers to `base`, which must outlive
+ * it.  Not available for the interpolated approach.                       */
+MMR_API int mmr_sho_phidiv_create(mmr_sho* base, int32_t nspha, int32_t nconc, const double* kspha_div,
+                                  const double* kconc_div, mmr_sho** out);
 
 /* Replaces sampHighOrder(..., approach = 1, opt): the SVD + NUFFT
  * interpolated encoding (useInterpWorker, sampHighOrder.m:314-359).  The

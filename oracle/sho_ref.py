@@ -150,8 +150,8 @@ class ShoRef:
     def setPhiDiv(self, ksphaDiv, kconcDiv):
         """sampHighOrder.m:590-622 (phase-derivative forward operator)."""
         o = self.ctranspose().ctranspose()
-        o.ksphaDiv = np.asarray(ksphaDiv, dtype=np.float64).reshape(np.shape(ksphaDiv)[0], -1, order="F")
-        o.kconcDiv = np.asarray(kconcDiv, dtype=np.float64).reshape(np.shape(kconcDiv)[0], -1, order="F")
+        o.ksphaDiv = np.asarray(ksphaDiv, dtype=np.float64).reshape(np.shape(ksphaDiv)[0], self.M, order="F")
+        o.kconcDiv = np.asarray(kconcDiv, dtype=np.float64).reshape(np.shape(kconcDiv)[0], self.M, order="F")
         return o
 
     def mtimes(self, x, chunk=1024):

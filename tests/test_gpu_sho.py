@@ -173,3 +173,39 @@ def test_interp_masked_and_sense_cgne(mm):
     x, *_ = mm.cgne(A, data, None, 6, opt)
     xr, *_ = cgne_ref(lambda v, tr: mrsampfunc(v, tr, Sr, Rr), data, None, 6, opt)
     assert rel(x, xr) < 1e-4
+
+
+# ---- setPhiDiv (sampHighOrder.m:590-622; tests.m:42-62) ----
+@pytest.mark.parametrize("nd", [1, 2, 3])
+def test_phidiv_vs_oracle(mm, nd):
+    rng = np.random.default_rng(20 + nd)
+    imN = [round(64 ** (2 / nd))] * nd
+    kN = [round(64 ** (1 / nd))] * nd
+    b0, t, spha, conc, grid = _rand_case(rng, imN, kN)
+    zs = np.zeros([16, 1] + kN[1:])
+    dspha = np.diff(np.concatenate([zs, spha], axis=1), axis=1)           # tests.m:43-48
+    dconc = np.diff(np.concatenate([np.zeros([4, 1] + kN[1:]), conc], axis=1), axis=1)
+    S = mm.sampHighOrder(b0, t, spha, conc, grid)
+    Sd = S.setPhiDiv(dspha, dconc)
+    R = ShoRef(b0, t, spha, conc, grid)
+    Rd = R.setPhiDiv(dspha, dconc)
+    x = crandn(rng, imN + [3])
+    y = crandn(rng, kN + [2])
+    ref = Rd.mtimes(x)
+    assert rel(Sd * x, ref) < 1e-5
+    assert rel(Sd.H * y, R.H.mtimes(y)) < 1e-5          # the adjoint ignores phiDiv
+    assert rel(S * x, R.mtimes(x)) < 1e-5               # value semantics: S itself is unchanged
+
+
+def test_phidiv_inside_sense(mm):
+    # forward model of findDelAuto's delay update: mrSampFunc(x, 'notransp', S.setPhiDiv(...), R)
+    from matmri_gb300 import synth
+    from oracle.sense_ref import RcvrRef, mrsampfunc
+    b0, t, spha, conc, grid = synth.highorder_inputs(N=32, M=1024, seed=3)
+    dspha = np.gradient(spha, axis=1)
+    S = mm.sampHighOrder(b0, t, spha, conc, grid).setPhiDiv(dspha, np.zeros((0, t.size)))
+    Rf = ShoRef(b0, t, spha, conc, grid).setPhiDiv(dspha, np.zeros((0, t.size)))
+    maps = synth.coil_maps(32, 4, 1)
+    img = synth.ellipse_phantom(32, 6, 2, complex_phase=True)
+    A = mm.mrSampOp(S, mm.rcvrOp(maps, 0))
+    assert rel(A(img, "notransp"), mrsampfunc(img, "notransp", Rf, RcvrRef(maps))) < 1e-5

@@ -61,6 +61,26 @@ def test_sho_adjoint(nd):
     assert abs(d1 - d2) / min(abs(d1), abs(d2)) < 1e-8
 
 
+def test_sho_phidiv_is_phase_derivative():
+    # setPhiDiv (sampHighOrder.m:590-622, used at 376-380): with phiDiv = the phase coefficients
+    # themselves and no B0, S_phiDiv x = d/da [exp(i a kbase).' x / sqrt(V)] at a = 1
+    rng = np.random.default_rng(9)
+    imN, kN = [12, 10], [200]
+    grid = {k: 0.1 * rng.standard_normal(imN) for k in "xyz"}
+    spha, conc = rng.standard_normal([16] + kN), rng.standard_normal([4] + kN)
+    t = np.linspace(0, 1, kN[0])
+    S = ShoRef(None, t, spha, conc, grid)
+    x = crandn(rng, imN)
+    h = 1e-5
+    fd = (ShoRef(None, t, (1 + h) * spha, (1 + h) * conc, grid).mtimes(x)
+          - ShoRef(None, t, (1 - h) * spha, (1 - h) * conc, grid).mtimes(x)) / (2 * h)
+    got = S.setPhiDiv(spha, conc).mtimes(x)
+    assert np.linalg.norm(got - fd) / np.linalg.norm(fd) < 1e-8
+    # the adjoint ignores phiDiv (369-372)
+    y = crandn(rng, kN)
+    assert np.allclose(S.setPhiDiv(spha, conc).H.mtimes(y), S.H.mtimes(y))
+
+
 def test_sho_fourier():
     # @sampHighOrder/tests.m:265-283: Cartesian linear phase == centered FFT (< 1e-10)
     N = 32

@@ -34,6 +34,14 @@ struct ShoPlan {
     bool tensor = true;     // with the table: tensor-core contraction (sho_tc.cu), else the SIMT kernels
     ShoTcScratch tc;
     std::shared_ptr<ShoInterp> interp;   // approach 1 (sho_interp.cu); the fields above stay empty
+    int nspha = 0, nconc = 0;
+    // setPhiDiv (sampHighOrder.m:590-622): a derived plan that refers to `base` (not owned) and
+    // holds the derivative phase d[v, m] = sum_j Bd[j][v] Pd[j][m] (prepForDirect with
+    // sampTimes = 1, i.e. no B0 term; sampHighOrder.m:376-380)
+    ShoPlan* base = nullptr;
+    int Kd = 0;
+    DevBuf d_Bd, d_Pd;      // double [Kd][V], [Kd][M]
+    DevBuf s_X, s_T;        // scratch: [V, Kd * chunk], [M, Kd * chunk]
     Staged st_in, st_out;
 };
 
@@ -211,7 +219,57 @@ __global__ void __launch_bounds__(256) sho_adj_kernel(const float* __restrict__ 
     }
 }
 
+// X[:, j + Kd b] = Bd[j] .* x[:, b]
+__global__ void phidiv_expand_kernel(const float2* __restrict__ x, const double* __restrict__ Bd,
+                                     float2* __restrict__ X, long long V, int Kd, long long nb, const int* active) {
+    if (active && *active) return;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= V * Kd * nb) return;
+    const long long v = i % V, col = i / V;
+    const int j = (int)(col % Kd);
+    const long long b = col / Kd;
+    X[i] = cscale(x[v + V * b], (float)Bd[(size_t)j * V + v]);
+}
+
+// y[m, b] = i sum_j Pd[j][m] T[m, j + Kd b]   (sampHighOrder.m:377-380)
+__global__ void phidiv_combine_kernel(const float2* __restrict__ T, const double* __restrict__ Pd,
+                                      float2* __restrict__ y, long long M, int Kd, long long nb, const int* active) {
+    if (active && *active) return;
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M * nb) return;
+    const long long m = i % M, b = i / M;
+    float re = 0.f, im = 0.f;
+    for (int j = 0; j < Kd; ++j) {
+        const float p = (float)Pd[(size_t)j * M + m];
+        const float2 t = T[m + M * (j + (long long)Kd * b)];
+        re += p * t.x;
+        im += p * t.y;
+    }
+    y[i] = make_float2(-im, re);
+}
+
+static void phidiv_forward(ShoPlan& s, const float2* x, float2* y, long long nb, cudaStream_t st,
+                           const int* active) {
+    const long long chunk = std::max<long long>(1, 256 / s.Kd);
+    s.s_X.ensure((size_t)s.V * s.Kd * chunk * sizeof(float2));
+    s.s_T.ensure((size_t)s.M * s.Kd * chunk * sizeof(float2));
+    for (long long b0 = 0; b0 < nb; b0 += chunk) {
+        const long long n = std::min(chunk, nb - b0);
+        phidiv_expand_kernel<<<(unsigned)cdiv(s.V * s.Kd * n, 256), 256, 0, st>>>(
+            x + s.V * b0, s.d_Bd.as<double>(), s.s_X.as<float2>(), s.V, s.Kd, n, active);
+        check_launch("phidiv_expand");
+        sho_forward(*s.base, s.s_X.as<float2>(), s.s_T.as<float2>(), s.Kd * n, st, active);
+        phidiv_combine_kernel<<<(unsigned)cdiv(s.M * n, 256), 256, 0, st>>>(
+            s.s_T.as<float2>(), s.d_Pd.as<double>(), y + s.M * b0, s.M, s.Kd, n, active);
+        check_launch("phidiv_combine");
+    }
+}
+
 void sho_forward(ShoPlan& s, const float2* x, float2* y, long long nb, cudaStream_t st, const int* active) {
+    if (s.base) {
+        phidiv_forward(s, x, y, nb, st, active);
+        return;
+    }
     if (s.interp) {
         sho_interp_forward(*s.interp, x, y, nb, st, active);
         return;
@@ -237,6 +295,10 @@ void sho_forward(ShoPlan& s, const float2* x, float2* y, long long nb, cudaStrea
 }
 
 void sho_adjoint(ShoPlan& s, const float2* y, float2* x, long long nb, cudaStream_t st, const int* active) {
+    if (s.base) {   // the adjoint ignores phiDiv (sampHighOrder.m:369-372)
+        sho_adjoint(*s.base, y, x, nb, st, active);
+        return;
+    }
     if (s.interp) {
         sho_interp_adjoint(*s.interp, y, x, nb, st, active);
         return;
@@ -274,6 +336,8 @@ static void sho_build(ShoPlan& s, const mmr_sho_desc& d) {
         s.V *= d.imN[k];
     }
     s.M = d.nsamp;
+    s.nspha = d.nspha;
+    s.nconc = d.nconc;
     const bool with_b0 = s.M > 1;                                          // 580
     s.K = d.nspha + d.nconc + (with_b0 ? 1 : 0);
     MMR_REQUIRE(s.K >= 1, "no phase terms");
@@ -356,6 +420,50 @@ extern "C" int mmr_sho_interp_create(const mmr_sho_interp_desc* desc, mmr_sho** 
             s->V = sho_interp_nvox(*s->interp);
             s->M = sho_interp_nsamp(*s->interp);
             s->tensor = false;
+        } catch (...) {
+            delete s;
+            throw;
+        }
+        *out = reinterpret_cast<mmr_sho*>(s);
+    });
+}
+
+extern "C" int mmr_sho_phidiv_create(mmr_sho* base_h, int32_t nspha, int32_t nconc, const double* kspha_div,
+                                     const double* kconc_div, mmr_sho** out) {
+    return guarded([&] {
+        MMR_REQUIRE(base_h && out, "NULL argument");
+        *out = nullptr;
+        ShoPlan& b = *reinterpret_cast<ShoPlan*>(base_h);
+        MMR_REQUIRE(!b.base, "the base plan already carries phiDiv");
+        MMR_REQUIRE(!b.interp, "phiDiv not yet implemented for interpolated approach");   // sampHighOrder.m:340-342
+        MMR_REQUIRE(nspha >= 0 && nconc >= 0 && nspha + nconc >= 1, "no phiDiv terms");
+        MMR_REQUIRE(nspha <= b.nspha && nconc <= b.nconc,
+                    "phiDiv has more terms than the plan's phs_spha / phs_conc");
+        MMR_REQUIRE((nspha == 0 || kspha_div) && (nconc == 0 || kconc_div), "missing phiDiv coefficients");
+        auto* s = new ShoPlan();
+        try {
+            s->base = &b;
+            s->nd = b.nd;
+            for (int k = 0; k < 3; ++k) s->imN[k] = b.imN[k];
+            s->V = b.V;
+            s->M = b.M;
+            s->Kd = nspha + nconc;
+            std::vector<double> Pd((size_t)s->Kd * s->M);
+            for (int j = 0; j < nspha; ++j)
+                for (long long m = 0; m < s->M; ++m) Pd[(size_t)j * s->M + m] = kspha_div[j + (size_t)nspha * m];
+            for (int j = 0; j < nconc; ++j)
+                for (long long m = 0; m < s->M; ++m)
+                    Pd[(size_t)(nspha + j) * s->M + m] = kconc_div[j + (size_t)nconc * m];
+            for (double v : Pd) MMR_REQUIRE(std::isfinite(v), "non-finite phiDiv coefficient");
+            s->d_Pd.upload(Pd);
+            // basis columns of the base plan: spherical harmonics 1..nspha, concomitant 1..nconc
+            s->d_Bd.ensure((size_t)s->Kd * s->V * sizeof(double));
+            const size_t col = (size_t)s->V * sizeof(double);
+            if (nspha)
+                MMR_CUDA(cudaMemcpy(s->d_Bd.p, b.d_B.p, (size_t)nspha * col, cudaMemcpyDeviceToDevice));
+            if (nconc)
+                MMR_CUDA(cudaMemcpy((char*)s->d_Bd.p + (size_t)nspha * col, (char*)b.d_B.p + (size_t)b.nspha * col,
+                                    (size_t)nconc * col, cudaMemcpyDeviceToDevice));
         } catch (...) {
             delete s;
             throw;

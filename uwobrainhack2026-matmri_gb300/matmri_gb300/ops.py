@@ -264,6 +264,7 @@ class sampHighOrder(_Op):
         if gx.ndim != 2:
             raise ValueError("the interpolated approach is built for 2-D grids (no SMS slice stacks)")
         t = np.asarray(sampTimes, dtype=np.float64)
+        self._t = t
         self.imSize = list(gx.shape)
         self.kSize = list(t.shape) if not (t.ndim == 2 and t.shape[1] == 1) else [t.shape[0]]
         if b0 is not None and np.size(b0) and np.size(b0) != gx.size:
@@ -293,6 +294,43 @@ class sampHighOrder(_Op):
         self._h = _Handle(h.value, lib.mmr_sho_destroy)
         self.V, self.M = gx.size, t.size
 
+    def setPhiDiv(self, ksphaDiv, kconcDiv):
+        """S2 = S.setPhiDiv(ksphaDiv, kconcDiv) (sampHighOrder.m:590-622), a copy (value semantics).
+
+        The copy's forward is (1i * exp(1i*kbase) .* phiDiv).' * x / sqrt(V)
+        (useDirectWorker, 374-381); its adjoint ignores phiDiv (369-372).
+        For the interpolated approach the forward raises, as the reference's
+        useInterpWorker does (340-342).
+        """
+        o = copy.copy(self)
+        o._phidiv_base = self
+        if self.approach == 1:
+            o._phidiv_unsupported = True
+            return o
+        ks = np.asarray(ksphaDiv, dtype=np.float64)
+        ks = np.zeros((0, self.M)) if ks.size == 0 else ks.reshape(ks.shape[0], -1, order="F")
+        kc = np.asarray(kconcDiv, dtype=np.float64) if kconcDiv is not None else np.zeros((0, self.M))
+        kc = np.zeros((0, self.M)) if kc.size == 0 else kc.reshape(kc.shape[0], -1, order="F")
+        if ks.shape[1] != self.M or kc.shape[1] != self.M:
+            raise ValueError("Dimension mismatch between phiDiv and sampTimes")
+        ks, kc = np.asfortranarray(ks), np.asfortranarray(kc)
+        o._keep_phidiv = (ks, kc)
+        lib = _lib.load()
+        h = C.c_void_p()
+        cp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double)) if a.size else None
+        _lib.check(lib.mmr_sho_phidiv_create(self.handle, ks.shape[0], kc.shape[0], cp(ks), cp(kc), C.byref(h)))
+        o._h = _Handle(h.value, lib.mmr_sho_destroy)
+        return o
+
+    def updateObj(self, phs_spha, phs_conc, b0map, b0mask, phs_grid):
+        """sampHighOrder.m:889-934: rebuilds the interpolated plan for new inputs (approach 1 only)."""
+        if self.approach != 1:
+            raise ValueError("this case not yet coded")                            # sampHighOrder.m:932
+        opt = {"svdThresh": self.svdThresh, "subFact": self.subFact}
+        o = copy.copy(self)
+        o._init_interp(b0map, self._t, phs_spha, phs_conc, phs_grid, b0mask, opt)
+        return o
+
     def set_tensor(self, on: bool = True):
         """Tensor-core contraction (default) or the SIMT FP32 kernels."""
         _lib.check(_lib.load().mmr_sho_set_tensor(self.handle, int(bool(on))))
@@ -303,6 +341,8 @@ class sampHighOrder(_Op):
         return self._h.ptr
 
     def mtimes(self, x):
+        if getattr(self, "_phidiv_unsupported", False) and not self.adjoint:
+            raise ValueError("phiDiv not yet implemented for interpolated approach")   # sampHighOrder.m:340-342
         lib = _lib.load()
         b = as_c64(x)
         shp = list(b.shape)

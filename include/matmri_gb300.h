@@ -183,6 +183,23 @@ typedef struct mmr_sho_interp_desc {
 } mmr_sho_interp_desc;
 MMR_API int mmr_sho_interp_create(const mmr_sho_interp_desc* desc, mmr_sho** out);
 
+/* ---- mrSampFuncMat (dense normal matrix) -------------------------------------
+ * Replaces [AtA, ~] = mrSampFuncMat(y, Crcvr, b0, sampTimes, phs_spha, phs_conc,
+ *   phs_grid, imMask) (operators/mrSampFuncMat.m:22-47) for the matrix part:
+ *   AtA = sum_c conj(r_c) r_c.' .* (S'*S),  S = exp(1i*kbase(vox,:)).'/sqrt(nvox)
+ * over the nvox voxels listed in vox (host, 0-based, column-major order; the
+ * imMask voxels).  S must be a direct sampHighOrder plan (mmr_sho_create),
+ * R an rcvrOp over the same image or NULL (single coil of ones).  AtA: device
+ * complex64 [nvox x nvox] column-major, written.  Aty = R'*(S'*y) on the mask
+ * comes from mmr_sense_apply.                                              */
+MMR_API int mmr_dense_normal(mmr_sho* S, mmr_rcvr* R, const int64_t* vox, int64_t nvox, void* AtA, void* stream);
+/* x = (AtA + lam2*I) \ b (demos/demo_denseMat.m:98-106) on device complex64
+ * buffers; AtA is not modified.  Cholesky, or LU with partial pivoting when
+ * the shifted matrix is not numerically positive definite; *method (may be
+ * NULL) receives 1 or 2 accordingly.  Synchronises the stream.             */
+MMR_API int mmr_dense_solve(const void* AtA, int64_t n, double lam2, const void* b, void* x, int32_t* method,
+                            void* stream);
+
 /* ---- mrSampFunc --------------------------------------------------------------
  * Replaces opFunc = @(x,transp) mrSampFunc(x, transp, S, R, opt)
  *   (operators/mrSampFunc.m:1-160) for S a nufftOp or sampHighOrder and R an

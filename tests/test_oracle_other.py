@@ -159,3 +159,28 @@ def test_torch_generators_match_numpy():
     mt = synth.coil_maps_torch(40, 6, 3, randomize=True, device="cpu")
     assert mt.shape == (40, 40, 6) and mt.stride() == (1, 40, 1600)
     assert np.abs(mt.numpy() - m).max() < 1e-6
+
+
+def test_dense_normal_matrix_equals_operator_normal():
+    # mrSampFuncMat.m:22-47 with a full mask: AtA x == R'S'SR x and Aty == R'S'y
+    from oracle.densemat_ref import mrsampfuncmat_ref
+    from oracle.sense_ref import RcvrRef, mrsampfunc
+    rng = np.random.default_rng(4)
+    N, M, C = 10, 150, 3
+    c = (np.arange(N) - N / 2) * 0.02
+    X, Y = np.meshgrid(c, c, indexing="ij")
+    grid = {"x": X, "y": Y, "z": np.zeros_like(X)}
+    spha = np.zeros((16, M))
+    spha[1:3] = rng.uniform(-150, 150, (2, M))
+    spha[4] = rng.uniform(-300, 300, M)
+    t = np.linspace(0, 0.01, M)
+    b0 = rng.uniform(-50, 50, (N, N))
+    maps = crandn(rng, (N, N, C))
+    y = crandn(rng, (M, C))
+    AtA, Aty = mrsampfuncmat_ref(y, maps, b0, t, spha, np.zeros((4, M)), grid)
+    S, R = ShoRef(b0, t, spha, np.zeros((4, M)), grid), RcvrRef(maps)
+    x = crandn(rng, (N, N))
+    ref = mrsampfunc(mrsampfunc(x, "notransp", S, R), "transp", S, R).reshape(-1, order="F")
+    assert np.linalg.norm(AtA @ x.reshape(-1, order="F") - ref) < 1e-10 * np.linalg.norm(ref)
+    assert np.allclose(Aty, mrsampfunc(y, "transp", S, R).reshape(-1, order="F"), atol=1e-12)
+    assert np.allclose(AtA, AtA.conj().T, atol=1e-12)

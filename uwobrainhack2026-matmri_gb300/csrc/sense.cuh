@@ -20,6 +20,8 @@ void sho_forward(ShoPlan& s, const float2* x, float2* y, long long nb, cudaStrea
 void sho_adjoint(ShoPlan& s, const float2* y, float2* x, long long nb, cudaStream_t st, const int* active);
 long long sho_nvox(const ShoPlan& s);
 long long sho_nsamp(const ShoPlan& s);
+// E [M, nvox] complex64, E[m + M j] = exp(i kbase[vox[j], m]) (vox: device indices).
+void sho_encoding_matrix(ShoPlan& s, const long long* vox, long long nvox, float2* E, cudaStream_t st);
 
 void rcvr_forward(const RcvrPlan& r, const float2* x, float2* y, cudaStream_t st, const int* active);
 void rcvr_adjoint(const RcvrPlan& r, const float2* y, float2* x, cudaStream_t st, const int* active);

@@ -323,6 +323,27 @@ void sho_adjoint(ShoPlan& s, const float2* y, float2* x, long long nb, cudaStrea
     check_launch("sho_adj");
 }
 
+// E[m + M j] = exp(i kbase[vox[j], m])   (mrSampFuncMat.m:35-37 before the 1/sqrt scaling)
+__global__ void sho_emat_kernel(const float* __restrict__ turn, const double* __restrict__ B,
+                                const double* __restrict__ P, int K, long long V, long long M,
+                                const long long* __restrict__ vox, long long nvox, float2* __restrict__ E) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= M * nvox) return;
+    const long long m = i % M, v = vox[i / M];
+    const float t = turn ? turn[v * M + m] : phase_turn(sho_phase(B, P, K, V, M, v, m));
+    float sn, cs;
+    sincospif(2.f * t, &sn, &cs);
+    E[i] = make_float2(cs, sn);
+}
+
+void sho_encoding_matrix(ShoPlan& s, const long long* vox, long long nvox, float2* E, cudaStream_t st) {
+    MMR_REQUIRE(!s.base && !s.interp, "the dense encoding needs a direct sampHighOrder plan");
+    sho_emat_kernel<<<(unsigned)cdiv(s.M * nvox, 256), 256, 0, st>>>(s.table ? s.d_turn.as<float>() : nullptr,
+                                                                     s.d_B.as<double>(), s.d_P.as<double>(), s.K,
+                                                                     s.V, s.M, vox, nvox, E);
+    check_launch("sho_emat");
+}
+
 static void sho_build(ShoPlan& s, const mmr_sho_desc& d) {
     MMR_REQUIRE(d.ndim >= 1 && d.ndim <= 3, "ndim must be 1..3");
     MMR_REQUIRE(d.nsamp >= 1 && d.t && d.spha && d.gx && d.gy && d.gz, "missing sampHighOrder input");

@@ -2,8 +2,8 @@
 
 Drop-in classes and functions with the reference's names and arguments:
 ``nufftOp``, ``rcvrOp``, ``sampHighOrder``, ``mrSampFunc`` (+ ``mrSampOp``),
-``cgne``, ``powermethod``, ``bfista``, ``dwtND``, ``findDelAuto`` and
-``interpTrajTime``.  All compute runs in
+``cgne``, ``powermethod``, ``bfista``, ``dwtND``, ``findDelAuto``,
+``interpTrajTime``, ``mrSampFuncMat`` (+ ``dense_solve``).  All compute runs in
 ``libmatmri_gb300.so`` (hand-written CUDA for sm_103a behind a C ABI); the
 package raises on import of an operator when the library is missing.
 """
@@ -13,6 +13,8 @@ from .sense import mrSampFunc, mrSampOp
 from .solvers import bfista, cgne, cgne_batch, dwtND, powermethod
 from .learned import PrecondNet, lpcg
 from .finddel import findDelAuto, interpTrajTime
+from .densemat import dense_solve, mrSampFuncMat
 
 __all__ = ["nufftOp", "rcvrOp", "sampHighOrder", "mrSampFunc", "mrSampOp", "cgne", "cgne_batch", "powermethod",
-           "bfista", "dwtND", "PrecondNet", "lpcg", "findDelAuto", "interpTrajTime", "MatmriError", "load_library"]
+           "bfista", "dwtND", "PrecondNet", "lpcg", "findDelAuto", "interpTrajTime", "mrSampFuncMat",
+           "dense_solve", "MatmriError", "load_library"]

@@ -123,6 +123,10 @@ SIGNATURES = {
     "mmr_sho_destroy": (C.c_int, [C.c_void_p]),
     "mmr_sho_set_tensor": (C.c_int, [C.c_void_p, C.c_int]),
     "mmr_sho_interp_create": (C.c_int, [C.POINTER(ShoInterpDesc), C.POINTER(C.c_void_p)]),
+    "mmr_dense_normal": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int64), C.c_int64, C.c_void_p,
+                                   C.c_void_p]),
+    "mmr_dense_solve": (C.c_int, [C.c_void_p, C.c_int64, C.c_double, C.c_void_p, C.c_void_p,
+                                  C.POINTER(C.c_int32), C.c_void_p]),
     "mmr_sho_phidiv_create": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(C.c_double),
                                         C.POINTER(C.c_double), C.POINTER(C.c_void_p)]),
     "mmr_sense_create": (C.c_int, [C.POINTER(SenseDesc), C.POINTER(C.c_void_p)]),

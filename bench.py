@@ -403,6 +403,99 @@ def highorder_measure(dev, reps=5, nit=30):
                              "rel_err_forward_vs_fp64_256_samples": rel1}}
 
 
+def finddel_measure(dev, cpu=True):
+    """findDelAuto (delay between a field trajectory and the data): wall time of a whole estimation on
+    the GPU at 64 x 64, 8 coils, 4096 samples, maxNit 15 (data simulated by the device encoding at a
+    0.37-dwell delay), and on a 32 x 32, 4-coil, 2048-sample case both on the GPU and with the FP64
+    restatement on the host cores."""
+    import torch
+    import matmri_gb300 as mm
+    from matmri_gb300 import synth
+
+    def case(N, C, M, delay=0.37):
+        c = synth.finddel_inputs(N, C, M, 3.0, 6.0, 7)
+        dt = c["datatime"]
+        S = mm.sampHighOrder(c["b0"], dt, c["phases"](dt + delay).T, np.zeros((4, M)), c["grid"])
+        data = mm.mrSampOp(S, mm.rcvrOp(c["maps"], 0))(c["img"], "notransp")
+        return c, np.asarray(data)
+
+    def run(c, data, impl):
+        args = (data, c["tdwell"], c["traj"], c["conc"], c["datatime"], c["grid"], c["b0"], c["maps"], 15)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        d, hist = impl(0.0, *args)
+        torch.cuda.synchronize()
+        return time.perf_counter() - t0, float(d), len(hist)
+
+    out = {"workload": "findDelAuto, maxNit 15, coarse search +-2 dwells, delay 0.37 dwell"}
+    c, data = case(64, 8, 4096)
+    run(c, data, mm.findDelAuto)                        # warm-up (library load, first plans)
+    s, d, n = run(c, data, mm.findDelAuto)
+    out["gpu_64x64_8coils_4096"] = {"s": s, "delay": d, "iterations": n - 1}
+    c, data = case(32, 4, 2048)
+    s, d, n = run(c, data, mm.findDelAuto)
+    small = {"gpu_s": s, "delay": d, "iterations": n - 1}
+    if cpu:
+        from oracle.finddel_ref import find_del_auto
+        s, d, n = run(c, data, find_del_auto)
+        small.update(cpu_s=s, cpu_delay=d, cpu_iterations=n - 1, cores=len(os.sched_getaffinity(0)),
+                     cpu_kind="port (FP64 restatement)")
+    out["32x32_4coils_2048"] = small
+    return out
+
+
+def dense_measure(dev, cpu=True):
+    """mrSampFuncMat at 128 x 128, 16384 samples, 16 coils (full mask): time to build the dense normal
+    matrix (16384^2 complex64; the Gram is 8 V^2 M = 35.2 TFLOP), its error against the iterative normal
+    operator on one image, and one Tikhonov direct solve; the host restatement's Gram time is measured on
+    a 1024-column slice and scaled to the full matrix."""
+    import torch
+    import matmri_gb300 as mm
+    from matmri_gb300 import synth
+    N, M, C = 128, 16384, 16
+    b0, t, spha, conc, grid = synth.highorder_inputs(N, M)
+    maps = synth.coil_maps(N, C, 3001)
+    img = synth.ellipse_phantom(N, 10, 3002, complex_phase=True)
+    A = mm.mrSampOp(mm.sampHighOrder(b0, t, spha, conc, grid), mm.rcvrOp(maps, 0))
+    y = A(_dev_cm(img, dev), "notransp")
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    AtA, Aty = mm.mrSampFuncMat(y, maps, b0, t, spha, conc, grid)
+    torch.cuda.synchronize()
+    t_build = time.perf_counter() - t0
+    x = _dev_cm(img, dev)
+    ref = A(A(x, "notransp"), "transp").T.reshape(-1)
+    got = AtA @ x.T.reshape(-1)
+    err = float(torch.linalg.vector_norm(got - ref) / torch.linalg.vector_norm(ref))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    xs, method = mm.dense_solve(AtA, Aty, 1e-2)
+    torch.cuda.synchronize()
+    t_solve = time.perf_counter() - t0
+    V = N * N
+    out = {"workload": "mrSampFuncMat 128x128, 16384 samples, 16 coils, full mask; (AtA + 1e-2 I) \\ Aty",
+           "s_build": t_build, "tflops_gram": 8.0 * V * V * M / t_build / 1e12, "rel_err_vs_operator": err,
+           "s_solve": t_solve, "solve_method": method}
+    del AtA, xs
+    torch.cuda.empty_cache()
+    if cpu:
+        from oracle.sho_ref import ShoRef
+        ref = ShoRef(b0, t, spha, conc, grid)
+        B, P = ref.basis_matrix()
+        t0 = time.perf_counter()
+        Ef = np.exp(1j * (B @ P[:, :2048]))            # all voxels x 2048 samples
+        t_e = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        G = Ef[:1024].conj() @ Ef.T                    # 1024 rows of the Gram over 2048 samples
+        t_g = time.perf_counter() - t0
+        out["cpu"] = {"s_build_extrapolated": t_e * (M / 2048) + t_g * (V / 1024) * (M / 2048),
+                      "sample": "FP64 numpy: the phases and exponentials of 2048 samples and a 1024 x 16384 x 2048 "
+                                "slice of the Gram, scaled to 16384 x 16384 x 16384",
+                      "cores": len(os.sched_getaffinity(0)), "kind": "port"}
+        del Ef, G
+    return out
+
+
 def run_reference(args):
     ws, rank, _ = dist_env()
     if rank != 0:
@@ -608,6 +701,8 @@ def main():
         if not args.no_extra:
             line["regridding"] = regridding_measure(dev)
             line["highorder"] = highorder_measure(dev)
+            line["finddel"] = finddel_measure(dev, cpu=not args.no_cpu_baseline)
+            line["dense"] = dense_measure(dev, cpu=not args.no_cpu_baseline)
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(case)
         print(json.dumps(line), flush=True)

@@ -59,48 +59,18 @@ def orient_grid(c, orient):
 
 
 def finddel_case(N=24, C=4, M=1536, true_delay=0.37, seed=7, snr=200.0, turns=3, wobble=2.0):
-    """A delay-estimation problem for findDelAuto (findDel/findDelAuto.m).
-
-    Data times are 20..20+M-1 (unit dwell); the field trajectory is tabulated
-    every 0.5 from t = 0 and the data are simulated with the exact phases at
-    t + true_delay (FP64 direct encoding, coil maps, complex Gaussian noise at
-    the given SNR).  The trajectory is a 3-turn spiral in the linear terms, a
-    constant term and two small second-order terms.
-    """
+    """A delay-estimation problem for findDelAuto (findDel/findDelAuto.m): the inputs of
+    synth.finddel_inputs with data simulated by the FP64 direct encoding at the exact phases of
+    t + true_delay, through the coil maps, plus complex Gaussian noise at the given SNR."""
     from oracle.sense_ref import RcvrRef
     from oracle.sho_ref import ShoRef
     from matmri_gb300 import synth
     rng = np.random.default_rng(seed)
-    fov = 0.22
-    c = (np.arange(N) - N / 2) * fov / N
-    X, Y = np.meshgrid(c, c, indexing="ij")
-    grid = {"x": X, "y": Y, "z": np.zeros_like(X)}
-    T = 20 + M + 40
-    kmax = np.pi * N / fov
-
-    def phases(t):
-        tau = t / T
-        r = kmax * tau
-        th = 2 * np.pi * turns * tau
-        sp = np.zeros((t.size, 16))
-        sp[:, 0] = wobble * np.sin(2 * np.pi * 8 * tau)
-        sp[:, 1] = r * np.cos(th)
-        sp[:, 2] = r * np.sin(th)
-        sp[:, 4] = 40.0 * tau ** 2
-        sp[:, 8] = -25.0 * tau
-        return sp
-
-    tdwell = 0.5
-    lenTraj = int(T / tdwell) + 1
-    traj = phases(tdwell * np.arange(lenTraj))
-    conc = np.zeros((lenTraj, 4))
-    datatime = 20.0 + np.arange(M, dtype=np.float64)
-    b0 = 2e-3 * np.exp(-((X - 0.03) ** 2 + (Y + 0.02) ** 2) / 0.004)      # rad per time unit
-    maps = synth.coil_maps(N, C, seed)
-    img = synth.ellipse_phantom(N, 6, seed + 1, complex_phase=True)
-    S = ShoRef(b0, datatime, phases(datatime + true_delay).T, np.zeros((4, M)), grid)
-    data = S.mtimes(RcvrRef(maps).mtimes(img))
+    c = synth.finddel_inputs(N, C, M, turns, wobble, seed)
+    dt = c["datatime"]
+    S = ShoRef(c["b0"], dt, c["phases"](dt + true_delay).T, np.zeros((4, M)), c["grid"])
+    data = S.mtimes(RcvrRef(c["maps"]).mtimes(c["img"]))
     sig = np.sqrt(np.mean(np.abs(data) ** 2)) / snr
     data = data + sig * (rng.standard_normal(data.shape) + 1j * rng.standard_normal(data.shape)) / np.sqrt(2)
-    return dict(data=data, tdwell=tdwell, traj=traj, conc=conc, datatime=datatime, grid=grid, b0=b0,
-                maps=maps, true_delay=true_delay)
+    c.update(data=data, true_delay=true_delay)
+    return c

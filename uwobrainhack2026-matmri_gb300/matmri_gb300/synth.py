@@ -221,3 +221,37 @@ def batched_cases(n_slices: int = 64, seed: int = 4000):
         samples = int(g.integers(2048, 4097))
         out.append(sense_case(N, C, n_int, samples, R=max(1.0, 16.0 / n_int), seed=seed + 10 * s + 1))
     return out
+
+
+def finddel_inputs(N: int = 24, C: int = 4, M: int = 1536, turns: float = 3.0, wobble: float = 6.0,
+                   seed: int = 7, fov: float = 0.22):
+    """Inputs of a delay-estimation problem (findDelAuto): data times 20..20+M-1 (unit dwell), a field
+    trajectory tabulated every 0.5 from t = 0 (a `turns`-turn spiral in the linear terms, a zeroth-order
+    phase oscillation of amplitude `wobble` rad and two small second-order terms), B0, coil maps and an
+    ellipse image.  `phases(t)` gives the exact coefficients [t.size, 16] at any time, so that data can be
+    simulated at t + delay."""
+    c = (np.arange(N) - N / 2) * fov / N
+    X, Y = np.meshgrid(c, c, indexing="ij")
+    grid = {"x": X, "y": Y, "z": np.zeros_like(X)}
+    T = 20 + M + 40
+    kmax = math.pi * N / fov
+
+    def phases(t):
+        tau = np.asarray(t, dtype=np.float64) / T
+        r = kmax * tau
+        th = 2 * math.pi * turns * tau
+        sp = np.zeros((tau.size, 16))
+        sp[:, 0] = wobble * np.sin(2 * math.pi * 8 * tau)
+        sp[:, 1] = r * np.cos(th)
+        sp[:, 2] = r * np.sin(th)
+        sp[:, 4] = 40.0 * tau ** 2
+        sp[:, 8] = -25.0 * tau
+        return sp
+
+    tdwell = 0.5
+    lenTraj = int(T / tdwell) + 1
+    return dict(tdwell=tdwell, traj=phases(tdwell * np.arange(lenTraj)), conc=np.zeros((lenTraj, 4)),
+                datatime=20.0 + np.arange(M, dtype=np.float64), grid=grid,
+                b0=2e-3 * np.exp(-((X - 0.03) ** 2 + (Y + 0.02) ** 2) / 0.004),
+                maps=coil_maps(N, C, seed), img=ellipse_phantom(N, 6, seed + 1, complex_phase=True),
+                phases=phases)

@@ -366,30 +366,29 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
     return false;
 }
 
-// Stage a [cg][R][R] complex region whose origin is (ox, oy) into smem.
-// TMA when the region is inside the grid, wrapped plain loads otherwise.
-__device__ __forceinline__ bool stage_region(float2* reg, const float2* __restrict__ grid, const CUtensorMap* tmap,
-                                             bool use_tma, uint64_t* bar, int ox, int oy, int c0, int cg, int R,
-                                             int G1, int G2, long long nb) {
-    // TMA only for regions fully inside the grid whose inner start (2*ox floats) is
-    // 16-byte aligned and whose row (2*R floats) is a multiple of 16 bytes.
+// TMA only for regions fully inside the grid whose inner start (2*ox floats) is
+// 16-byte aligned and whose row (2*R floats) is a multiple of 16 bytes.  Thread 0
+// issues the copy; returns whether it did (the caller then waits on `bar`).
+__device__ __forceinline__ bool region_issue(float2* reg, const CUtensorMap* tmap, bool use_tma, uint64_t* bar,
+                                             int ox, int oy, int c0, int cg, int R, int G1, int G2) {
     const bool inside = use_tma && ox >= 0 && oy >= 0 && ox + R <= G1 && oy + R <= G2 && (ox & 1) == 0 &&
                         (R & 1) == 0;
-    if (inside) {
-        if (threadIdx.x == 0) {
-            const uint32_t bytes = (uint32_t)cg * R * R * 8;
-            asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-                         : "memory");
-            asm volatile(
-                "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
-                "%4}], [%5];" ::"r"(smem_u32(reg)),
-                "l"(tmap), "r"(2 * ox), "r"(oy), "r"(c0), "r"(smem_u32(bar))
-                : "memory");
-        }
-        const bool ok = mbar_wait(bar, 0);
-        return ok;
+    if (inside && threadIdx.x == 0) {
+        const uint32_t bytes = (uint32_t)cg * R * R * 8;
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                     : "memory");
+        asm volatile(
+            "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+            "%4}], [%5];" ::"r"(smem_u32(reg)),
+            "l"(tmap), "r"(2 * ox), "r"(oy), "r"(c0), "r"(smem_u32(bar))
+            : "memory");
     }
-    // wrapped rows: one warp per (coil, row), lanes along the row
+    return inside;
+}
+
+// Wrapped plain loads of the region: one warp per (coil, row), lanes along the row.
+__device__ __forceinline__ void region_plain(float2* reg, const float2* __restrict__ grid, int ox, int oy, int c0,
+                                             int cg, int R, int G1, int G2, long long nb) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
     for (int cr = warp; cr < cg * R; cr += nwarp) {
         const int c = cr / R, ry = cr - c * R;
@@ -407,6 +406,15 @@ __device__ __forceinline__ bool stage_region(float2* reg, const float2* __restri
         }
     }
     __syncthreads();
+}
+
+// Stage a [cg][R][R] complex region whose origin is (ox, oy) into smem.
+// TMA when the region is inside the grid, wrapped plain loads otherwise.
+__device__ __forceinline__ bool stage_region(float2* reg, const float2* __restrict__ grid, const CUtensorMap* tmap,
+                                             bool use_tma, uint64_t* bar, int ox, int oy, int c0, int cg, int R,
+                                             int G1, int G2, long long nb) {
+    if (region_issue(reg, tmap, use_tma, bar, ox, oy, c0, cg, R, G1, G2)) return mbar_wait(bar, 0);
+    region_plain(reg, grid, ox, oy, c0, cg, R, G1, G2, nb);
     return true;
 }
 
@@ -660,36 +668,46 @@ __global__ void __launch_bounds__(256) gridnorm2d_binned(const float2* __restric
     zero_acc(acc, 2 * a.cg * PS);
     const int e0 = item.y, e1 = item.z;
     mbar_init(bar);
+    // interpolated, weighted samples [entry][coil], after the accumulators of a full tile, then the
+    // batch's entry lists staged in shared memory: sample index, base cell, the 2W tap weights
+    float2* sval = reinterpret_cast<float2*>(acc + (size_t)2 * a.cg * acc_plane(a.T));
+    int* es = reinterpret_cast<int*>(sval + (size_t)a.chunk * a.cg);
+    short2* elb = reinterpret_cast<short2*>(es + a.chunk);
+    float* ew = reinterpret_cast<float*>(elb + a.chunk);
+    // the region copy is issued first and waited for after the entry lists are loaded; the
+    // tensor map's box is a full tile's region, so sub-tiles use plain loads
+    bool tma = false;
     if (e1 > e0) {
-        // the tensor map's box is a full tile's region: sub-tiles use plain loads
-        if (!stage_region(reg, gin, &tmap, a.use_tma && T == a.T, bar, u0 - W, v0 - W, c0, a.cg, R, a.G1, a.G2,
-                          a.nb))
-            return;
+        tma = region_issue(reg, &tmap, a.use_tma && T == a.T, bar, u0 - W, v0 - W, c0, a.cg, R, a.G1, a.G2);
+        if (!tma) region_plain(reg, gin, u0 - W, v0 - W, c0, a.cg, R, a.G1, a.G2, a.nb);
     }
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
     constexpr int off0 = -W / 2 + 1;
-    // interpolated, weighted samples [entry][coil], after the accumulators of a full tile
-    float2* sval = reinterpret_cast<float2*>(acc + (size_t)2 * a.cg * acc_plane(a.T));
     int lgcg = 0;
     while ((1 << lgcg) < a.cg) ++lgcg;
-    // entries are processed in batches of a.chunk (the capacity of sval)
+    // entries are processed in batches of a.chunk (the capacity of sval and the entry lists)
     for (int eb = e0; eb < e1; eb += a.chunk) {
-    const int ee = min(e1, eb + a.chunk);
+    const int ee = min(e1, eb + a.chunk), ne = ee - eb;
+    for (int i = threadIdx.x; i < ne; i += blockDim.x) {
+        es[i] = a.ent_s[eb + i];
+        elb[i] = a.ent_lb[eb + i];
+    }
+    __syncthreads();
+    for (int j = threadIdx.x; j < ne * 2 * W; j += blockDim.x) {
+        const int i = j / (2 * W), k = j - i * (2 * W);
+        ew[j] = a.wts[(size_t)es[i] * 2 * W + k];
+    }
+    if (eb == e0 && tma && !mbar_wait(bar, 0)) return;
+    __syncthreads();
     // phase 1 — interpolation, one thread per (entry, coil), separable weights:
     //   v = sum_b w2[b] sum_a w1[a] g[b][a]; independent loads, no shuffles, no atomics
-    const int npair = (ee - eb) << lgcg;
+    const int npair = ne << lgcg;
     for (int p = threadIdx.x; p < npair; p += blockDim.x) {
-        const int e = eb + (p >> lgcg), c = p & (a.cg - 1);
-        const int s = a.ent_s[e];
-        const short2 lb = a.ent_lb[e];
-        const float* w = a.wts + (size_t)s * 2 * W;
-        float w1[W], w2[W];
-#pragma unroll
-        for (int i = 0; i < W; ++i) {
-            w1[i] = w[i];
-            w2[i] = w[W + i];
-        }
+        const int i = p >> lgcg, c = p & (a.cg - 1);
+        const short2 lb = elb[i];
+        const float* w1 = ew + i * 2 * W;
+        const float* w2 = w1 + W;
         const float2* rc = reg + (size_t)c * R * R + (lb.y + off0 + W) * R + (lb.x + off0 + W);
         float2 v = make_float2(0.f, 0.f);
 #pragma unroll
@@ -705,28 +723,27 @@ __global__ void __launch_bounds__(256) gridnorm2d_binned(const float2* __restric
             v.y += w2[b] * row.y;
         }
         float f = 1.f;
-        if (a.wfac && c0 + c < a.nb) f = a.wfac[s + a.wfac_bstride * (c0 + c)];
+        if (a.wfac && c0 + c < a.nb) f = a.wfac[es[i] + a.wfac_bstride * (c0 + c)];
         sval[p] = make_float2(v.x * f, v.y * f);
     }
     __syncthreads();
     // phase 2 — spreading, one lane per tap; the entry's taps are decoded once per warp
     const int grp = lane / TM::LPP, gl = lane % TM::LPP;
-    for (int e = eb + warp; e < ee; e += nwarp) {
-        const int s = a.ent_s[e];
-        const short2 lb = a.ent_lb[e];
-        const float* w = a.wts + (size_t)s * 2 * W;
+    for (int i = warp; i < ne; i += nwarp) {
+        const short2 lb = elb[i];
+        const float* w = ew + i * 2 * W;
         float wt[TM::TPL];
         int ao[TM::TPL];
 #pragma unroll
-        for (int i = 0; i < TM::TPL; ++i) {
-            const int k = gl + i * TM::LPP;
+        for (int t = 0; t < TM::TPL; ++t) {
+            const int k = gl + t * TM::LPP;
             const int ta = k % W, tb = k / W;
             const int l1 = lb.x + off0 + ta, l2 = lb.y + off0 + tb;
             const bool ok = k < TM::TAPS && l1 >= 0 && l1 < te1 && l2 >= 0 && l2 < te2;
-            wt[i] = ok ? w[ta] * w[W + tb] : 0.f;
-            ao[i] = ok ? l2 * RS + l1 : -1;
+            wt[t] = ok ? w[ta] * w[W + tb] : 0.f;
+            ao[t] = ok ? l2 * RS + l1 : -1;
         }
-        const float2* sv = sval + ((e - eb) << lgcg);
+        const float2* sv = sval + (i << lgcg);
         for (int cb = 0; cb < a.cg; cb += TM::PPW) {
             const int c = cb + grp;
             if (c >= a.cg || c0 + c >= a.nb) continue;
@@ -734,10 +751,10 @@ __global__ void __launch_bounds__(256) gridnorm2d_binned(const float2* __restric
             float* re = acc + (size_t)c * PS;
             float* im = re + (size_t)a.cg * PS;
 #pragma unroll
-            for (int i = 0; i < TM::TPL; ++i) {
-                if (ao[i] >= 0) {
-                    atomicAdd(re + ao[i], wt[i] * v.x);
-                    atomicAdd(im + ao[i], wt[i] * v.y);
+            for (int t = 0; t < TM::TPL; ++t) {
+                if (ao[t] >= 0) {
+                    atomicAdd(re + ao[t], wt[t] * v.x);
+                    atomicAdd(im + ao[t], wt[t] * v.y);
                 }
             }
         }
@@ -960,7 +977,8 @@ void nufft_grid_normal(NufftPlan& p, const float2* gin, float2* gout, long long 
                        cudaStream_t st, const int* active) {
     MMR_REQUIRE(p.use_bins, "fused gridding needs the 2D binned path");
     const int T = p.bins.T, R = T + 2 * p.W;
-    const int cg = pick_cg(p, nb, ((size_t)R * R + acc_plane_host(T) + p.bins.chunk) * 8, kTmaSmemExtra);
+    const size_t ent = (size_t)p.bins.chunk * (8 + 8 * p.W);    // staged entry lists (gridnorm2d_binned)
+    const int cg = pick_cg(p, nb, ((size_t)R * R + acc_plane_host(T) + p.bins.chunk) * 8, kTmaSmemExtra + ent);
     static const void* cptr = nullptr;
     static long long cnb = 0;
     static int ccg = 0, cR = 0, cG1 = 0, cG2 = 0;
@@ -973,7 +991,7 @@ void nufft_grid_normal(NufftPlan& p, const float2* gin, float2* gout, long long 
         cG1 = p.G[0];
         cG2 = p.G[1];
     }
-    const size_t smem = kTmaSmemExtra + (size_t)cg * ((size_t)R * R + acc_plane_host(T) + p.bins.chunk) * 8;
+    const size_t smem = kTmaSmemExtra + ent + (size_t)cg * ((size_t)R * R + acc_plane_host(T) + p.bins.chunk) * 8;
     Bin2DArgs a = bin_args(p, false, wfac, wfb, nb, cg, true, active);
     dim3 gridDim((unsigned)p.bins.n_pad_items, (unsigned)cdiv(nb, cg));
     zero_shared(p, gout, nb, st, active);

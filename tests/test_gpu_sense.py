@@ -197,3 +197,27 @@ def test_normal_modes(mm, mode, kw):
     x = crandn(rng, (96, 96))
     ref = mrsampfunc(mrsampfunc(x, "notransp", Sr, Rr), "transp", Sr, Rr, opt)
     assert rel(op.normal(x), ref) < TOL
+
+
+@pytest.mark.parametrize("tile,cgrp,item", [(8, 1, 8), (16, 2, 16), (32, 2, 128), (32, 4, 64), (64, 8, 256)])
+def test_fused_normal_work_items(mm, tile, cgrp, item):
+    # fused gridding over a variable-density spiral (dense centre: quadtree sub-tiles and leaves
+    # shared by several items; empty corner tiles) for every tile / coil-group / item size
+    from matmri_gb300 import synth
+    N, C = 96, 6
+    kloc = synth.spiral(N, 4, 2048, 2)
+    M = kloc.shape[0]
+    rng = np.random.default_rng(tile + cgrp + item)
+    maps = synth.coil_maps(N, C, 3)
+    S = mm.nufftOp([N, N], kloc, None, 1, 2.0, 4)
+    R = mm.rcvrOp(maps, 0)
+    Sr = NufftRef([N, N], kloc, None, 2.0, 4)
+    Rr = RcvrRef(maps)
+    W = rng.uniform(0.5, 1.5, M)
+    opt = {"W": W}
+    op = mm.mrSampOp(S, R, opt)
+    op.set_tuning(0, tile, cgrp, item, 0, 1)
+    assert op.get_tuning()[1:4] == (tile, cgrp, item) and op.get_tuning()[5] == 1
+    x = crandn(rng, (N, N))
+    ref = mrsampfunc(mrsampfunc(x, "notransp", Sr, Rr), "transp", Sr, Rr, opt)
+    assert rel(op.normal(x), ref) < TOL

@@ -65,12 +65,13 @@ __global__ void __launch_bounds__(256) fft_pass_kernel(const PassArgs a) {
     int lgB = 0;
     while ((1 << lgB) < B) ++lgB;
     const int ls = padded_len(L);
-    float2* buf0 = sm;
-    float2* buf1 = sm + B * ls;
     const int tid = threadIdx.x, nt = blockDim.x;
 
     // ---- tile decomposition
     const bool contiguous = (MODE != PASS_ADJ_COMBINE) && a.inner == 1;
+    const int bufw = fft_buf_words(L, B);
+    float2* buf0 = sm;
+    float2* buf1 = sm + bufw;
     long long l0 = 0, q0 = 0, o = 0;
     int coil = 0;
     if (contiguous) {
@@ -114,13 +115,14 @@ __global__ void __launch_bounds__(256) fft_pass_kernel(const PassArgs a) {
             if (contiguous) a.out[t + (long long)a.nout * (l0 + b)] = v;
             else a.out[(q0 + b) + a.inner * (t + (long long)a.nout * o)] = v;
         };
-        run_fft<LC, SIGN>(buf0, buf1, a.tw, a.f, B, lgB, ls, !contiguous, ld, stf);
+        if (contiguous) run_fft<LC, SIGN, false>(buf0, buf1, a.tw, a.f, B, lgB, ls, ld, stf);
+        else run_fft<LC, SIGN, true>(buf0, buf1, a.tw, a.f, B, lgB, ls, ld, stf);
         return;
     }
 
     // ---- ADJ_COMBINE: crop, deapod, conj(maps) into a staging tile, then a deterministic
     //      coil sum across the thread-block cluster through distributed shared memory
-    float2* stg = sm + 2 * B * ls;
+    float2* stg = sm + 2 * bufw;
     auto stc = [&](int b, int n, float2 v) {
         int t = n - a.out_start;
         t += (t < 0) ? L : 0;
@@ -133,7 +135,7 @@ __global__ void __launch_bounds__(256) fft_pass_kernel(const PassArgs a) {
         }
         stg[t * B + b] = r;
     };
-    run_fft<LC, SIGN>(buf0, buf1, a.tw, a.f, B, lgB, ls, true, ld, stc);
+    run_fft<LC, SIGN, true>(buf0, buf1, a.tw, a.f, B, lgB, ls, ld, stc);
     cg::cluster_group cl = cg::this_cluster();
     cl.sync();
     const int cs = (int)cl.num_blocks();
@@ -163,7 +165,7 @@ __global__ void __launch_bounds__(256) fft_pass_kernel(const PassArgs a) {
 
 template <int MODE, int SIGN, int LC>
 static void launch_mode(const PassArgs& a, cudaStream_t st) {
-    const size_t smem = (size_t)(2 * a.B * padded_len(a.L) + (MODE == PASS_ADJ_COMBINE ? a.B * a.L : 0)) *
+    const size_t smem = (size_t)(2 * fft_buf_words(a.L, a.B) + (MODE == PASS_ADJ_COMBINE ? a.B * a.L : 0)) *
                         sizeof(float2);
     auto kern = fft_pass_kernel<MODE, SIGN, LC>;
     static bool attr_done = false;   // one per instantiation

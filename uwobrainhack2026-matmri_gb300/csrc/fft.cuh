@@ -175,25 +175,39 @@ __device__ __forceinline__ void apply_twiddles(float2* v, const float2* __restri
     }
 }
 
-// Shared-memory index with one pad slot per 16 entries: breaks the stride-R
-// bank conflicts of the Stockham scatter.
+// Shared-memory layouts of the B lines a block transforms (B * padded_len(L) float2
+// per buffer either way; one pad slot per 16 entries).
+//  * line-major (contiguous axes; consecutive threads take consecutive butterflies of
+//    one line): element n of line b at b * ls + n + n / 16, ls = padded_len(L).  The
+//    pad slots break the stride-R bank conflicts of the Stockham scatter.
+//  * interleaved (strided axes; consecutive threads take consecutive lines): element n
+//    of line b at (n + n / 16) * B + b.  A half-warp (16 threads, one 8-byte access each)
+//    covers 16 / B consecutive butterflies of B lines: the stage reads and the later
+//    scatters fall on 16 distinct bank pairs, the radix-8 first-stage scatter on 8.  The
+//    line-major layout put up to 3 threads of a half-warp on one bank pair there.
 __device__ __forceinline__ int pidx(int i) { return i + (i >> 4); }
 __host__ __device__ __forceinline__ int padded_len(int L) { return L + (L >> 4) + 1; }
+// float2 words of one of the two ping-pong buffers
+__host__ __device__ __forceinline__ int fft_buf_words(int L, int B) { return B * padded_len(L); }
+template <bool TR>
+__device__ __forceinline__ int sidx(int b, int n, int ls, int B) {
+    return TR ? pidx(n) * B + b : b * ls + pidx(n);
+}
 
 // One Stockham stage over B lines.  FIRST reads its inputs through `ld(b, n)`
 // (natural index n, straight from global memory); LAST hands its outputs to
 // `stf(b, n, v)`; the stages in between read `src` and write `dst` (shared
-// memory, line stride ls, padded indices).  `bfast`: consecutive threads
-// take consecutive lines (strided axes), else consecutive butterflies.
-template <int R, int SIGN, bool FIRST, bool LAST, class Ld, class St>
+// memory, layout sidx<TR>).  TR: consecutive threads take consecutive lines
+// (strided axes, interleaved layout), else consecutive butterflies (line-major).
+template <int R, int SIGN, bool FIRST, bool LAST, bool TR, class Ld, class St>
 __device__ __forceinline__ void stockham_stage(const float2* __restrict__ src, float2* __restrict__ dst,
                                                const float2* __restrict__ tw, int L, int Ns, int B, int lgB, int ls,
-                                               bool bfast, const Ld& ld, const St& stf) {
+                                               const Ld& ld, const St& stf) {
     const int nbf = L / R;
     const int tws = L / (Ns * R);
     for (int w = threadIdx.x; w < nbf * B; w += blockDim.x) {
         int b, j;
-        if (bfast) { b = w & (B - 1); j = w >> lgB; }
+        if (TR) { b = w & (B - 1); j = w >> lgB; }
         else { b = w / nbf; j = w - b * nbf; }
         const int k = j % Ns;
         float2 v[R];
@@ -201,9 +215,8 @@ __device__ __forceinline__ void stockham_stage(const float2* __restrict__ src, f
 #pragma unroll
             for (int r = 0; r < R; ++r) v[r] = ld(b, j + r * nbf);
         } else {
-            const float2* s = src + b * ls;
 #pragma unroll
-            for (int r = 0; r < R; ++r) v[r] = s[pidx(j + r * nbf)];
+            for (int r = 0; r < R; ++r) v[r] = src[sidx<TR>(b, j + r * nbf, ls, B)];
         }
         if (!FIRST && Ns > 1) apply_twiddles<R, SIGN>(v, tw, k * tws);
         dftR<R, SIGN>(v);
@@ -212,38 +225,37 @@ __device__ __forceinline__ void stockham_stage(const float2* __restrict__ src, f
 #pragma unroll
             for (int r = 0; r < R; ++r) stf(b, base + r * Ns, v[r]);
         } else {
-            float2* d = dst + b * ls;
 #pragma unroll
-            for (int r = 0; r < R; ++r) d[pidx(base + r * Ns)] = v[r];
+            for (int r = 0; r < R; ++r) dst[sidx<TR>(b, base + r * Ns, ls, B)] = v[r];
         }
     }
 }
 
-template <int R, int SIGN, class Ld, class St>
+template <int R, int SIGN, bool TR, class Ld, class St>
 __device__ __forceinline__ void run_stage(int s, int nstage, const float2* src, float2* dst, const float2* tw, int L,
-                                          int Ns, int B, int lgB, int ls, bool bfast, const Ld& ld, const St& stf) {
+                                          int Ns, int B, int lgB, int ls, const Ld& ld, const St& stf) {
     const bool first = s == 0, last = s == nstage - 1;
-    if (first && last) stockham_stage<R, SIGN, true, true>(src, dst, tw, L, Ns, B, lgB, ls, bfast, ld, stf);
-    else if (first) stockham_stage<R, SIGN, true, false>(src, dst, tw, L, Ns, B, lgB, ls, bfast, ld, stf);
-    else if (last) stockham_stage<R, SIGN, false, true>(src, dst, tw, L, Ns, B, lgB, ls, bfast, ld, stf);
-    else stockham_stage<R, SIGN, false, false>(src, dst, tw, L, Ns, B, lgB, ls, bfast, ld, stf);
+    if (first && last) stockham_stage<R, SIGN, true, true, TR>(src, dst, tw, L, Ns, B, lgB, ls, ld, stf);
+    else if (first) stockham_stage<R, SIGN, true, false, TR>(src, dst, tw, L, Ns, B, lgB, ls, ld, stf);
+    else if (last) stockham_stage<R, SIGN, false, true, TR>(src, dst, tw, L, Ns, B, lgB, ls, ld, stf);
+    else stockham_stage<R, SIGN, false, false, TR>(src, dst, tw, L, Ns, B, lgB, ls, ld, stf);
 }
 
 // Runs all stages of B length-L transforms: input from ld, output to stf,
-// intermediates ping-pong between a and b (each B * ls float2).
-template <int SIGN, class Ld, class St>
+// intermediates ping-pong between a and b (each fft_buf_words(L, B, TR) float2).
+template <int SIGN, bool TR, class Ld, class St>
 __device__ void fft_lines(float2* a, float2* b, const float2* tw, const FftFactors& f, int B, int lgB, int ls,
-                          bool bfast, const Ld& ld, const St& stf) {
+                          const Ld& ld, const St& stf) {
     int Ns = 1;
     for (int s = 0; s < f.nstage; ++s) {
         const int R = f.radix[s];
         switch (R) {
-            case 8: run_stage<8, SIGN>(s, f.nstage, a, b, tw, f.L, Ns, B, lgB, ls, bfast, ld, stf); break;
-            case 4: run_stage<4, SIGN>(s, f.nstage, a, b, tw, f.L, Ns, B, lgB, ls, bfast, ld, stf); break;
-            case 2: run_stage<2, SIGN>(s, f.nstage, a, b, tw, f.L, Ns, B, lgB, ls, bfast, ld, stf); break;
-            case 3: run_stage<3, SIGN>(s, f.nstage, a, b, tw, f.L, Ns, B, lgB, ls, bfast, ld, stf); break;
-            case 5: run_stage<5, SIGN>(s, f.nstage, a, b, tw, f.L, Ns, B, lgB, ls, bfast, ld, stf); break;
-            case 7: run_stage<7, SIGN>(s, f.nstage, a, b, tw, f.L, Ns, B, lgB, ls, bfast, ld, stf); break;
+            case 8: run_stage<8, SIGN, TR>(s, f.nstage, a, b, tw, f.L, Ns, B, lgB, ls, ld, stf); break;
+            case 4: run_stage<4, SIGN, TR>(s, f.nstage, a, b, tw, f.L, Ns, B, lgB, ls, ld, stf); break;
+            case 2: run_stage<2, SIGN, TR>(s, f.nstage, a, b, tw, f.L, Ns, B, lgB, ls, ld, stf); break;
+            case 3: run_stage<3, SIGN, TR>(s, f.nstage, a, b, tw, f.L, Ns, B, lgB, ls, ld, stf); break;
+            case 5: run_stage<5, SIGN, TR>(s, f.nstage, a, b, tw, f.L, Ns, B, lgB, ls, ld, stf); break;
+            case 7: run_stage<7, SIGN, TR>(s, f.nstage, a, b, tw, f.L, Ns, B, lgB, ls, ld, stf); break;
             default: break;
         }
         __syncthreads();
@@ -270,18 +282,35 @@ __host__ __device__ constexpr int cradix(int L, int s) {
 __host__ __device__ constexpr int cns(int L, int s) { return s == 0 ? 1 : cns(L, s - 1) * cradix(L, s - 1); }
 __host__ __device__ constexpr bool fft_has_cplan(int L) { return cnstage(L) > 0; }
 
-template <int L, int S, int SIGN, class Ld, class St>
+// Offset (in float2, before the factor B of the interleaved layout) of element r of a
+// butterfly's reads (n = j + r * nbf) and writes (n = base + r * Ns) from its element 0,
+// when the pad slots make it a compile-time constant; -1 otherwise.  It holds for every
+// line, butterfly and r of the compile-time plans where it is not -1: a stride that is
+// a multiple of 16 shifts the pad count by a constant; a first-stage radix dividing 16
+// keeps the R outputs of a butterfly inside one 16-entry group; a write stride of 8
+// with an even radix starts every butterfly's group in the lower half of a 16-entry block.
+__host__ __device__ constexpr int rd_off(int nbf, int r) { return nbf % 16 == 0 ? r * nbf + r * nbf / 16 : -1; }
+__host__ __device__ constexpr int wr_off(int R, int Ns, int r) {
+    return Ns == 1 ? (16 % R == 0 ? r : -1)
+         : Ns % 16 == 0 ? r * Ns + r * Ns / 16
+         : (Ns == 8 && R % 2 == 0) ? 8 * r + r / 2
+         : -1;
+}
+
+template <int L, int S, int SIGN, bool TR, class Ld, class St>
 __device__ __forceinline__ void cstage(const float2* __restrict__ src, float2* __restrict__ dst,
-                                       const float2* __restrict__ tw, int B, int lgB, int ls, bool bfast, const Ld& ld,
+                                       const float2* __restrict__ tw, int B, int lgB, int ls, const Ld& ld,
                                        const St& stf) {
     constexpr int R = cradix(L, S);
     constexpr int Ns = cns(L, S);
     constexpr bool FIRST = S == 0, LAST = S == cnstage(L) - 1;
     constexpr int nbf = L / R;
     constexpr int tws = L / (Ns * R);
+    constexpr bool RDC = rd_off(nbf, 1) >= 0, WRC = wr_off(R, Ns, 1) >= 0;
+    const int m = TR ? B : 1;   // offset multiplier of the layout
     for (int w = threadIdx.x; w < nbf * B; w += blockDim.x) {
         int b, j;
-        if (bfast) { b = w & (B - 1); j = w >> lgB; }
+        if (TR) { b = w & (B - 1); j = w >> lgB; }
         else { b = w / nbf; j = w - b * nbf; }
         const int k = j % Ns;
         float2 v[R];
@@ -289,9 +318,14 @@ __device__ __forceinline__ void cstage(const float2* __restrict__ src, float2* _
 #pragma unroll
             for (int r = 0; r < R; ++r) v[r] = ld(b, j + r * nbf);
         } else {
-            const float2* s = src + b * ls;
+            if constexpr (RDC) {
+                const float2* s0 = src + sidx<TR>(b, j, ls, B);
 #pragma unroll
-            for (int r = 0; r < R; ++r) v[r] = s[pidx(j + r * nbf)];
+                for (int r = 0; r < R; ++r) v[r] = s0[rd_off(nbf, r) * m];
+            } else {
+#pragma unroll
+                for (int r = 0; r < R; ++r) v[r] = src[sidx<TR>(b, j + r * nbf, ls, B)];
+            }
             if constexpr (Ns > 1) apply_twiddles<R, SIGN>(v, tw, k * tws);
         }
         dftR<R, SIGN>(v);
@@ -299,30 +333,34 @@ __device__ __forceinline__ void cstage(const float2* __restrict__ src, float2* _
         if (LAST) {
 #pragma unroll
             for (int r = 0; r < R; ++r) stf(b, base + r * Ns, v[r]);
-        } else {
-            float2* d = dst + b * ls;
+        } else if constexpr (WRC) {
+            float2* d0 = dst + sidx<TR>(b, base, ls, B);
 #pragma unroll
-            for (int r = 0; r < R; ++r) d[pidx(base + r * Ns)] = v[r];
+            for (int r = 0; r < R; ++r) d0[wr_off(R, Ns, r) * m] = v[r];
+        } else {
+#pragma unroll
+            for (int r = 0; r < R; ++r) dst[sidx<TR>(b, base + r * Ns, ls, B)] = v[r];
         }
     }
 }
 
-template <int L, int S, int SIGN, class Ld, class St>
-__device__ __forceinline__ void cstages(float2* a, float2* b, const float2* tw, int B, int lgB, int ls, bool bfast,
+template <int L, int S, int SIGN, bool TR, class Ld, class St>
+__device__ __forceinline__ void cstages(float2* a, float2* b, const float2* tw, int B, int lgB, int ls,
                                         const Ld& ld, const St& stf) {
     if constexpr (S < cnstage(L)) {
-        cstage<L, S, SIGN>(a, b, tw, B, lgB, ls, bfast, ld, stf);
+        cstage<L, S, SIGN, TR>(a, b, tw, B, lgB, ls, ld, stf);
         __syncthreads();
-        cstages<L, S + 1, SIGN>(b, a, tw, B, lgB, ls, bfast, ld, stf);
+        cstages<L, S + 1, SIGN, TR>(b, a, tw, B, lgB, ls, ld, stf);
     }
 }
 
-// LC = compile-time length (0: runtime plan f).
-template <int LC, int SIGN, class Ld, class St>
+// LC = compile-time length (0: runtime plan f).  TR: interleaved layout, consecutive
+// threads on consecutive lines (strided axes).
+template <int LC, int SIGN, bool TR, class Ld, class St>
 __device__ __forceinline__ void run_fft(float2* a, float2* b, const float2* tw, const FftFactors& f, int B, int lgB,
-                                        int ls, bool bfast, const Ld& ld, const St& stf) {
-    if constexpr (LC == 0) fft_lines<SIGN>(a, b, tw, f, B, lgB, ls, bfast, ld, stf);
-    else cstages<LC, 0, SIGN>(a, b, tw, B, lgB, ls, bfast, ld, stf);
+                                        int ls, const Ld& ld, const St& stf) {
+    if constexpr (LC == 0) fft_lines<SIGN, TR>(a, b, tw, f, B, lgB, ls, ld, stf);
+    else cstages<LC, 0, SIGN, TR>(a, b, tw, B, lgB, ls, ld, stf);
 }
 
 // Launch a pass (host). `cluster` > 1 only for PASS_ADJ_COMBINE.

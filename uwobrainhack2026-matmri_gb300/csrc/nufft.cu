@@ -195,6 +195,7 @@ void nufft_build_bins(NufftPlan& p, int Treq, int chunk) {
     if (p.nd != 2) return;
     MMR_REQUIRE(chunk >= 8, "work-item chunk must be >= 8");
     MMR_REQUIRE(p.G[0] < 65536 && p.G[1] < 65536, "grid too large for the binned path");
+    MMR_REQUIRE(p.G[0] % 2 == 0, "the binned path needs an even first grid extent");
     p.bins.chunk = chunk;
     int T = Treq;
     while (T >= 8 && (p.G[0] < 2 * (T + 2 * p.W) || p.G[1] < 2 * (T + 2 * p.W))) T /= 2;
@@ -546,17 +547,23 @@ __device__ __forceinline__ void flush_tile(const float* acc, float2* __restrict_
     const int lgT = 31 - __clz(T);
     const int PS = acc_plane(T), RS = acc_row(T);
     const float* im = acc + (size_t)a.cg * PS;
-    const int n = a.cg << (2 * lgT);
+    // two horizontally adjacent cells per iteration: T, te1 and the grid's first extent are
+    // even (osN is, nufftOp.m:146-152), so a pair is valid as a whole, its accumulators are
+    // float2-aligned and its grid cells float4-aligned
+    const int lgh = 2 * lgT - 1;
+    const int n = a.cg << lgh;
     for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const int c = i >> (2 * lgT), r = i & ((1 << (2 * lgT)) - 1), l2 = r >> lgT, l1 = r & (T - 1);
+        const int c = i >> lgh, r = (i & ((1 << lgh) - 1)) << 1, l2 = r >> lgT, l1 = r & (T - 1);
         if (l1 < te1 && l2 < te2 && c0 + c < a.nb) {
             float2* d = out + (u0 + l1) + (long long)a.G1 * ((v0 + l2) + (long long)a.G2 * (c0 + c));
             const int k = c * PS + l2 * RS + l1;
-            const float2 v = make_float2(acc[k], im[k]);
+            const float2 re = *reinterpret_cast<const float2*>(acc + k);
+            const float2 iv = *reinterpret_cast<const float2*>(im + k);
             if (!shared) {
-                *d = v;
-            } else if (v.x != 0.f || v.y != 0.f) {
-                atomicAdd(d, v);
+                *reinterpret_cast<float4*>(d) = make_float4(re.x, iv.x, re.y, iv.y);
+            } else {
+                if (re.x != 0.f || iv.x != 0.f) atomicAdd(d, make_float2(re.x, iv.x));
+                if (re.y != 0.f || iv.y != 0.f) atomicAdd(d + 1, make_float2(re.y, iv.y));
             }
         }
     }
@@ -648,58 +655,77 @@ __global__ void __launch_bounds__(256) spread2d_binned(const float2* __restrict_
     flush_tile(acc, grid, shared, T, u0, v0, te1, te2, c0, a);
 }
 
+// Zeroes an owned (sub)tile of the coil group's output planes (an item no sample touches).
+__device__ __forceinline__ void zero_tile(float2* __restrict__ out, int T, int u0, int v0, int te1, int te2, int c0,
+                                          const Bin2DArgs& a) {
+    const int lgT = 31 - __clz(T), lgh = 2 * lgT - 1;   // cell pairs, as in flush_tile
+    const int n = a.cg << lgh;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        const int c = i >> lgh, r = (i & ((1 << lgh) - 1)) << 1, l2 = r >> lgT, l1 = r & (T - 1);
+        if (l1 < te1 && l2 < te2 && c0 + c < a.nb)
+            *reinterpret_cast<float4*>(out + (u0 + l1) + (long long)a.G1 * ((v0 + l2) + (long long)a.G2 * (c0 + c))) =
+                make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+}
+
+// Shared-memory float2 words of the input region / accumulator area per coil: the
+// accumulators reuse the region once interpolation is done.
+__host__ __device__ __forceinline__ int gn_area(int T, int W) {
+    const int R = T + 2 * W, ps = (T + 4) * T + 16;   // acc_plane(T) floats, per real / imaginary plane
+    return R * R > ps ? R * R : ps;
+}
+
+// Fused normal operator on the grid, out = C^H diag(wfac) C in per coil (nufftOp.m:354-394
+// without the FFTs): one CTA per (work item, coil group).  The item's padded entries (at most
+// `chunk`: items are built that way) are interpolated from the staged input region, weighted,
+// and spread into the (sub)tile's accumulators, which alias the region.
 template <int W>
 __global__ void __launch_bounds__(256) gridnorm2d_binned(const float2* __restrict__ gin, float2* __restrict__ gout,
                                                          const Bin2DArgs a, const __grid_constant__ CUtensorMap tmap) {
     using TM = TapMap<W>;
     extern __shared__ float4 sm4[];
     if (a.active && *a.active) return;
-    const int R0 = a.T + 2 * W;                // region side of a full tile (smem layout)
-    uint64_t* bar;
-    float2* reg = tma_layout(sm4, &bar);
-    float* acc = reinterpret_cast<float*>(reg + (size_t)a.cg * R0 * R0);
     const int4 item = a.items[blockIdx.x];
     const int T = item.w & 255, R = T + 2 * W; // this item's (sub)tile and region sides
     const bool shared = (item.w >> 8) != 0;    // tile split across several items
     const int u0 = item.x & 0xffff, v0 = item.x >> 16;
     const int c0 = blockIdx.y * a.cg;
     const int te1 = min(T, a.G1 - u0), te2 = min(T, a.G2 - v0);
+    const int e0 = item.y, ne = item.z - item.y;
+    if (ne == 0) {
+        zero_tile(gout, T, u0, v0, te1, te2, c0, a);
+        return;
+    }
     const int PS = acc_plane(T), RS = acc_row(T);
-    zero_acc(acc, 2 * a.cg * PS);
-    const int e0 = item.y, e1 = item.z;
-    mbar_init(bar);
-    // interpolated, weighted samples [entry][coil], after the accumulators of a full tile, then the
-    // batch's entry lists staged in shared memory: sample index, base cell, the 2W tap weights
-    float2* sval = reinterpret_cast<float2*>(acc + (size_t)2 * a.cg * acc_plane(a.T));
+    uint64_t* bar;
+    float2* reg = tma_layout(sm4, &bar);
+    float* acc = reinterpret_cast<float*>(reg);
+    // interpolated, weighted samples [entry][coil], then the entry lists: sample index,
+    // base cell, the 2W tap weights
+    float2* sval = reg + (size_t)a.cg * gn_area(a.T, W);
     int* es = reinterpret_cast<int*>(sval + (size_t)a.chunk * a.cg);
     short2* elb = reinterpret_cast<short2*>(es + a.chunk);
     float* ew = reinterpret_cast<float*>(elb + a.chunk);
+    mbar_init(bar);
     // the region copy is issued first and waited for after the entry lists are loaded; the
     // tensor map's box is a full tile's region, so sub-tiles use plain loads
-    bool tma = false;
-    if (e1 > e0) {
-        tma = region_issue(reg, &tmap, a.use_tma && T == a.T, bar, u0 - W, v0 - W, c0, a.cg, R, a.G1, a.G2);
-        if (!tma) region_plain(reg, gin, u0 - W, v0 - W, c0, a.cg, R, a.G1, a.G2, a.nb);
-    }
-    __syncthreads();
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
-    constexpr int off0 = -W / 2 + 1;
-    int lgcg = 0;
-    while ((1 << lgcg) < a.cg) ++lgcg;
-    // entries are processed in batches of a.chunk (the capacity of sval and the entry lists)
-    for (int eb = e0; eb < e1; eb += a.chunk) {
-    const int ee = min(e1, eb + a.chunk), ne = ee - eb;
+    const bool tma = region_issue(reg, &tmap, a.use_tma && T == a.T, bar, u0 - W, v0 - W, c0, a.cg, R, a.G1, a.G2);
+    if (!tma) region_plain(reg, gin, u0 - W, v0 - W, c0, a.cg, R, a.G1, a.G2, a.nb);
     for (int i = threadIdx.x; i < ne; i += blockDim.x) {
-        es[i] = a.ent_s[eb + i];
-        elb[i] = a.ent_lb[eb + i];
+        es[i] = a.ent_s[e0 + i];
+        elb[i] = a.ent_lb[e0 + i];
     }
     __syncthreads();
     for (int j = threadIdx.x; j < ne * 2 * W; j += blockDim.x) {
         const int i = j / (2 * W), k = j - i * (2 * W);
         ew[j] = a.wts[(size_t)es[i] * 2 * W + k];
     }
-    if (eb == e0 && tma && !mbar_wait(bar, 0)) return;
+    if (tma && !mbar_wait(bar, 0)) return;
     __syncthreads();
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+    constexpr int off0 = -W / 2 + 1;
+    int lgcg = 0;
+    while ((1 << lgcg) < a.cg) ++lgcg;
     // phase 1 — interpolation, one thread per (entry, coil), separable weights:
     //   v = sum_b w2[b] sum_a w1[a] g[b][a]; independent loads, no shuffles, no atomics
     const int npair = ne << lgcg;
@@ -726,6 +752,8 @@ __global__ void __launch_bounds__(256) gridnorm2d_binned(const float2* __restric
         if (a.wfac && c0 + c < a.nb) f = a.wfac[es[i] + a.wfac_bstride * (c0 + c)];
         sval[p] = make_float2(v.x * f, v.y * f);
     }
+    __syncthreads();
+    zero_acc(acc, 2 * a.cg * PS);   // the region is no longer read
     __syncthreads();
     // phase 2 — spreading, one lane per tap; the entry's taps are decoded once per warp
     const int grp = lane / TM::LPP, gl = lane % TM::LPP;
@@ -758,8 +786,6 @@ __global__ void __launch_bounds__(256) gridnorm2d_binned(const float2* __restric
                 }
             }
         }
-    }
-    __syncthreads();
     }
     __syncthreads();
     flush_tile(acc, gout, shared, T, u0, v0, te1, te2, c0, a);
@@ -978,7 +1004,8 @@ void nufft_grid_normal(NufftPlan& p, const float2* gin, float2* gout, long long 
     MMR_REQUIRE(p.use_bins, "fused gridding needs the 2D binned path");
     const int T = p.bins.T, R = T + 2 * p.W;
     const size_t ent = (size_t)p.bins.chunk * (8 + 8 * p.W);    // staged entry lists (gridnorm2d_binned)
-    const int cg = pick_cg(p, nb, ((size_t)R * R + acc_plane_host(T) + p.bins.chunk) * 8, kTmaSmemExtra + ent);
+    const size_t per_coil = ((size_t)gn_area(T, p.W) + p.bins.chunk) * 8;    // region / accumulators, samples
+    const int cg = pick_cg(p, nb, per_coil, kTmaSmemExtra + ent);
     static const void* cptr = nullptr;
     static long long cnb = 0;
     static int ccg = 0, cR = 0, cG1 = 0, cG2 = 0;
@@ -991,7 +1018,7 @@ void nufft_grid_normal(NufftPlan& p, const float2* gin, float2* gout, long long 
         cG1 = p.G[0];
         cG2 = p.G[1];
     }
-    const size_t smem = kTmaSmemExtra + ent + (size_t)cg * ((size_t)R * R + acc_plane_host(T) + p.bins.chunk) * 8;
+    const size_t smem = kTmaSmemExtra + ent + (size_t)cg * per_coil;
     Bin2DArgs a = bin_args(p, false, wfac, wfb, nb, cg, true, active);
     dim3 gridDim((unsigned)p.bins.n_pad_items, (unsigned)cdiv(nb, cg));
     zero_shared(p, gout, nb, st, active);

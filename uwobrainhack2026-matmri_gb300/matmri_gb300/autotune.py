@@ -5,8 +5,11 @@ one pass stay resident in L2), gridding tile side (``tile``), coils per CTA in
 the gridding kernels (``coil_group``), samples per gridding work item
 (``item``) and transform lines per CTA in the FFT passes (``fft_lines``).
 
-The search is a coordinate descent from the current setting: each knob in
-turn is swept over its candidates with the others fixed, for two rounds.
+The search is a coordinate descent per gridding mode (fused interpolate /
+spread, or the precomputed stencil): from the current setting with that mode,
+each other knob in turn is swept over its candidates with the rest fixed, for
+two rounds; the faster mode's optimum wins.  (One descent over all knobs can
+stall in the slower mode: its optimum for the other knobs differs.)
 Every candidate is applied once untimed, then timed end to end with CUDA
 events around back-to-back normal operators (``mmr_sense_normal``), best of
 three.  Results are cached per size class (image
@@ -93,21 +96,31 @@ def autotune(op, reps=5, rounds=2, use_cache=True, verbose=False) -> dict:
     n = int(np.prod(op.imN))
     x = torch.randn(n, dtype=torch.complex64, device="cuda")
     y = torch.empty_like(x)
-    cur = dict(zip(["coil_chunk", "tile", "coil_group", "item", "fft_lines", "normal_mode"], op.get_tuning()))
-    best_t = time_normal(op, x.data_ptr(), y.data_ptr(), reps)
-    for _ in range(rounds):
-        for knob in ORDER:
-            for v in SPACE[knob]:
-                if v == cur[knob] or (knob == "coil_chunk" and v > op.C):
+    start = dict(zip(["coil_chunk", "tile", "coil_group", "item", "fft_lines", "normal_mode"], op.get_tuning()))
+    best_t, best = float("inf"), None
+    for mode in SPACE["normal_mode"]:
+        cur = dict(start, normal_mode=mode)
+        op.set_tuning(**cur)
+        cur_t = time_normal(op, x.data_ptr(), y.data_ptr(), reps)
+        for _ in range(rounds):
+            for knob in ORDER:
+                if knob == "normal_mode":
                     continue
-                trial = dict(cur, **{knob: v})
-                op.set_tuning(**trial)
-                t = time_normal(op, x.data_ptr(), y.data_ptr(), reps)
-                if verbose:
-                    print(f"autotune {trial} -> {t:.4f} ms")
-                if t < best_t:
-                    best_t, cur = t, trial
-            op.set_tuning(**cur)
+                for v in SPACE[knob]:
+                    if v == cur[knob] or (knob == "coil_chunk" and v > op.C):
+                        continue
+                    trial = dict(cur, **{knob: v})
+                    op.set_tuning(**trial)
+                    t = time_normal(op, x.data_ptr(), y.data_ptr(), reps)
+                    if verbose:
+                        print(f"autotune {trial} -> {t:.4f} ms")
+                    if t < cur_t:
+                        cur_t, cur = t, trial
+                op.set_tuning(**cur)
+        if cur_t < best_t:
+            best_t, best = cur_t, cur
+    cur = best
+    op.set_tuning(**cur)
     if use_cache:
         cache[key] = {"tuning": cur, "normal_ms": best_t}
         os.makedirs(os.path.dirname(path), exist_ok=True)

@@ -270,8 +270,11 @@ void nufft_build_bins(NufftPlan& p, int Treq, int chunk) {
         }
         return true;
     };
+    std::vector<float> wts((size_t)2 * p.W * p.M);
+    MMR_CUDA(cudaMemcpy(wts.data(), p.d_w.p, wts.size() * sizeof(float), cudaMemcpyDeviceToHost));
     std::vector<int> ps;
     std::vector<short2> plb;
+    std::vector<float> pw;
     std::vector<int2> heavy;   // {u0 | v0 << 16, side} of leaf tiles shared by several items
     items.clear();
     b.max_pad = 0;
@@ -294,6 +297,7 @@ void nufft_build_bins(NufftPlan& p, int Treq, int chunk) {
             ps.push_back(s);
             plb.push_back(make_short2((short)sdist((long long)base[s] - u0, p.G[0]),
                                       (short)sdist((long long)base[p.M + s] - v0, p.G[1])));
+            pw.insert(pw.end(), wts.begin() + (size_t)s * 2 * p.W, wts.begin() + (size_t)(s + 1) * 2 * p.W);
         }
         b.max_pad = std::max(b.max_pad, (int)list.size());
         const int e1 = (int)ps.size();
@@ -310,6 +314,7 @@ void nufft_build_bins(NufftPlan& p, int Treq, int chunk) {
     b.n_heavy = (int)heavy.size();
     b.pad_s.upload(ps);
     b.pad_lb.upload(plb);
+    b.pad_w.upload(pw);
     b.n_pad = (long long)ps.size();
     b.pad_items.upload(items);
     b.n_pad_items = (int)items.size();
@@ -460,6 +465,7 @@ struct Bin2DArgs {
     const int4* items;       // {u0 | v0 << 16, e0, e1, tile side}
     const int* ent_s;
     const short2* ent_lb;
+    const float* ent_w;      // padded lists: [entry][2][W] (the entry's sample's tap weights)
     const float* wts;        // [M][2][W]
     const float* wfac;       // per-sample weight or null
     long long wfac_bstride;  // 0 or M
@@ -701,34 +707,40 @@ __global__ void __launch_bounds__(256) gridnorm2d_binned(const float2* __restric
     float2* reg = tma_layout(sm4, &bar);
     float* acc = reinterpret_cast<float*>(reg);
     // interpolated, weighted samples [entry][coil], then the entry lists: sample index,
-    // base cell, the 2W tap weights
+    // base cell, the 2W tap weights, the per-sample weight of each (entry, coil)
     float2* sval = reg + (size_t)a.cg * gn_area(a.T, W);
     int* es = reinterpret_cast<int*>(sval + (size_t)a.chunk * a.cg);
     short2* elb = reinterpret_cast<short2*>(es + a.chunk);
     float* ew = reinterpret_cast<float*>(elb + a.chunk);
+    float* ef = ew + (size_t)a.chunk * 2 * W;
     mbar_init(bar);
     // the region copy is issued first and waited for after the entry lists are loaded; the
     // tensor map's box is a full tile's region, so sub-tiles use plain loads
     const bool tma = region_issue(reg, &tmap, a.use_tma && T == a.T, bar, u0 - W, v0 - W, c0, a.cg, R, a.G1, a.G2);
     if (!tma) region_plain(reg, gin, u0 - W, v0 - W, c0, a.cg, R, a.G1, a.G2, a.nb);
+    // the item's lists and inline tap weights are contiguous: independent, coalesced loads
     for (int i = threadIdx.x; i < ne; i += blockDim.x) {
         es[i] = a.ent_s[e0 + i];
         elb[i] = a.ent_lb[e0 + i];
     }
-    __syncthreads();
-    for (int j = threadIdx.x; j < ne * 2 * W; j += blockDim.x) {
-        const int i = j / (2 * W), k = j - i * (2 * W);
-        ew[j] = a.wts[(size_t)es[i] * 2 * W + k];
-    }
-    if (tma && !mbar_wait(bar, 0)) return;
+    for (int j = threadIdx.x; j < ne * 2 * W; j += blockDim.x) ew[j] = a.ent_w[(size_t)e0 * 2 * W + j];
     __syncthreads();
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
     constexpr int off0 = -W / 2 + 1;
     int lgcg = 0;
     while ((1 << lgcg) < a.cg) ++lgcg;
+    const int npair = ne << lgcg;
+    // the weights are gathered by sample index while the region copy completes
+    if (a.wfac) {
+        for (int q = threadIdx.x; q < npair; q += blockDim.x) {
+            const int i = q >> lgcg, c = q & (a.cg - 1);
+            ef[q] = c0 + c < a.nb ? a.wfac[es[i] + a.wfac_bstride * (c0 + c)] : 0.f;
+        }
+    }
+    if (tma && !mbar_wait(bar, 0)) return;
+    __syncthreads();
     // phase 1 — interpolation, one thread per (entry, coil), separable weights:
     //   v = sum_b w2[b] sum_a w1[a] g[b][a]; independent loads, no shuffles, no atomics
-    const int npair = ne << lgcg;
     for (int p = threadIdx.x; p < npair; p += blockDim.x) {
         const int i = p >> lgcg, c = p & (a.cg - 1);
         const short2 lb = elb[i];
@@ -748,8 +760,7 @@ __global__ void __launch_bounds__(256) gridnorm2d_binned(const float2* __restric
             v.x += w2[b] * row.x;
             v.y += w2[b] * row.y;
         }
-        float f = 1.f;
-        if (a.wfac && c0 + c < a.nb) f = a.wfac[es[i] + a.wfac_bstride * (c0 + c)];
+        const float f = a.wfac ? ef[p] : 1.f;
         sval[p] = make_float2(v.x * f, v.y * f);
     }
     __syncthreads();
@@ -897,6 +908,7 @@ static Bin2DArgs bin_args(const NufftPlan& p, bool own, const float* wfac, long 
     a.items = own ? b.own_items.as<int4>() : b.pad_items.as<int4>();
     a.ent_s = own ? b.own_s.as<int>() : b.pad_s.as<int>();
     a.ent_lb = own ? b.own_lb.as<short2>() : b.pad_lb.as<short2>();
+    a.ent_w = own ? nullptr : b.pad_w.as<float>();
     a.wts = p.d_w.as<float>();
     a.wfac = wfac;
     a.wfac_bstride = wfb;
@@ -1004,7 +1016,8 @@ void nufft_grid_normal(NufftPlan& p, const float2* gin, float2* gout, long long 
     MMR_REQUIRE(p.use_bins, "fused gridding needs the 2D binned path");
     const int T = p.bins.T, R = T + 2 * p.W;
     const size_t ent = (size_t)p.bins.chunk * (8 + 8 * p.W);    // staged entry lists (gridnorm2d_binned)
-    const size_t per_coil = ((size_t)gn_area(T, p.W) + p.bins.chunk) * 8;    // region / accumulators, samples
+    // per coil: region / accumulators, interpolated samples, per-sample weights
+    const size_t per_coil = ((size_t)gn_area(T, p.W) + p.bins.chunk) * 8 + (size_t)p.bins.chunk * 4;
     const int cg = pick_cg(p, nb, per_coil, kTmaSmemExtra + ent);
     static const void* cptr = nullptr;
     static long long cnb = 0;

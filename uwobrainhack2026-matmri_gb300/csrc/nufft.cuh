@@ -19,6 +19,7 @@ struct BinLists {
     int ntx = 0, nty = 0;
     DevBuf own_s, own_lb;            // interp: each sample once (tile containing its base cell)
     DevBuf pad_s, pad_lb;            // spread/normal: every (sub)tile its footprint touches
+    DevBuf pad_w;                    // float [n_pad][2][W]: each padded entry's tap weights
     DevBuf own_items, pad_items;     // int4 {u0 | v0 << 16, e0, e1, tile side | shared << 8}
     DevBuf heavy;                    // int2 {u0 | v0 << 16, side}: leaf tiles split across items
     int n_own_items = 0, n_pad_items = 0, n_heavy = 0;

@@ -353,6 +353,42 @@ def regridding_measure(dev, reps=200):
             "cpu_fp64_us_per_pair": t_cpu * 1e6, "cpu_cores": len(os.sched_getaffinity(0))}
 
 
+def toeplitz_measure(dev, reps=20, cpu_coils=4):
+    """Toeplitz normal operator (nufftOp.prepToep, nufftOp.m:410-432 and 348-352) on the 256 x 256,
+    32-coil, 4 x 4096 spiral case: microseconds per 32-coil S*x of the Toeplitz copy, beside the
+    gridding normal operator S'*(S*x) of the same batch; the Toeplitz transfer function's set-up
+    time; its error against the FP64 restatement on `cpu_coils` coils and the restatement's time
+    for those coils on the host cores (set-up and application)."""
+    import matmri_gb300 as mm
+    import oracle.nufft_ref as nr
+    case = make_case()
+    kloc, img, maps = case["kloc"], case["img"], case["maps"]
+    S = mm.nufftOp([N_IMG, N_IMG], kloc, None, 1, 2.0, 4)
+    t0 = time.perf_counter()
+    T = S.prepToep()
+    setup_s = time.perf_counter() - t0
+    x = (img[:, :, None] * maps).astype(np.complex64)
+    xd = _dev_cm(x, dev)
+    SH = S.H
+    us_toep = 1e3 * _timed_ms(lambda: T * xd, reps, dev)
+    us_grid = 1e3 * _timed_ms(lambda: SH * (S * xd), reps, dev)
+    yt = (T * xd).cpu().numpy()
+    yg = (SH * (S * xd)).cpu().numpy()
+    t0 = time.perf_counter()
+    Tr = nr.NufftRef([N_IMG, N_IMG], kloc, None, 2.0, 4).prepToep()
+    yr = Tr.mtimes(x[:, :, :cpu_coils])
+    t_cpu = time.perf_counter() - t0
+    err = float(np.linalg.norm(yt[:, :, :cpu_coils] - yr) / np.linalg.norm(yr))
+    gap = float(np.linalg.norm(yt - yg) / np.linalg.norm(yg))
+    return {"workload": "Toeplitz normal operator 256x256 (2N = 512 transfer function), 32 coils, "
+                        "4x4096 spiral R=4, kwidth 4, os 2 (tos 1.5)",
+            "us_toeplitz_32coils": us_toep, "us_gridding_normal_32coils": us_grid,
+            "speedup_vs_gridding": us_grid / us_toep, "setup_s": setup_s,
+            "rel_err_vs_fp64": err, "rel_diff_toeplitz_vs_gridding": gap,
+            "cpu_fp64_s_setup_plus_apply": t_cpu, "cpu_coils": cpu_coils,
+            "cpu_cores": len(os.sched_getaffinity(0))}
+
+
 def highorder_measure(dev, reps=5, nit=30):
     """High-order encoding: 128 x 128, single-shot spiral of 16384 samples, 16 spherical-harmonic
     terms, B0 +-100 Hz, 30 ms readout, 16 coils.  Times the 16-coil S*x and S'*y and a cgne solve of
@@ -705,6 +741,7 @@ def main():
             line["batched"] = batched_comparison(dev)
         if not args.no_extra:
             line["regridding"] = regridding_measure(dev)
+            line["toeplitz"] = toeplitz_measure(dev)
             line["highorder"] = highorder_measure(dev)
             line["finddel"] = finddel_measure(dev, cpu=not args.no_cpu_baseline)
             line["dense"] = dense_measure(dev, cpu=not args.no_cpu_baseline)

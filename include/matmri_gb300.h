@@ -229,7 +229,7 @@ MMR_API int mmr_sense_normal(mmr_sense* a, const void* in, void* out, void* stre
 MMR_API int mmr_sense_profile_normal(mmr_sense* a, const void* in, void* out, int32_t reps,
                                      double* stage_ms, int32_t* launches, void* stream);
 /* Tuning knobs chosen by the autotuner (0 = keep / automatic):
- *   coil_chunk  coils per pipeline pass (1..16; their grids stay L2-resident)
+ *   coil_chunk  coils per pipeline pass (1..32; their grids stay L2-resident)
  *   tile        gridding tile side (8, 16, 32, 64)
  *   coil_group  coils per CTA in the gridding kernels (1, 2, 4, 8)
  *   item        max samples per gridding work item (>= 8)

@@ -71,6 +71,19 @@ def test_coil_chunks(mm, chunk):
     assert rel(op(y, "transp"), mrsampfunc(y, "transp", Sr, Rr)) < TOL
 
 
+def test_coil_chunk_32(mm):
+    # all 32 coils in one pipeline pass
+    S, R, Sr, Rr, rng = _setup(mm, N=64, C=32, M=3000, seed=9)
+    op = mm.mrSampOp(S, R)
+    op.set_tuning(32, 0)
+    assert op.get_tuning()[0] == 32
+    x = crandn(rng, (64, 64))
+    ref = mrsampfunc(mrsampfunc(x, "notransp", Sr, Rr), "transp", Sr, Rr)
+    assert rel(op.normal(x), ref) < TOL
+    y = crandn(rng, (3000, 32))
+    assert rel(op(y, "transp"), mrsampfunc(y, "transp", Sr, Rr)) < TOL
+
+
 def test_opt_W_and_vectorised(mm):
     S, R, Sr, Rr, rng = _setup(mm, C=4, seed=7)
     W = rng.uniform(0, 2, 3000 * 4)      # vectorised data: W matches x(:) (mrSampFunc.m:126-128)

@@ -1,14 +1,11 @@
 // FFT pass kernels: Stockham radix stages in shared memory with fused
 // prologue (deapodisation, coil-map multiply, zero padding) and epilogue
-// (crop, deapodisation, conj-map multiply and a deterministic coil sum
-// across a thread-block cluster through distributed shared memory).
+// (crop, deapodisation, scaling).
 #include <cmath>
 #include <map>
 #include <mutex>
 
 #include "fft.cuh"
-
-namespace cg = cooperative_groups;
 
 namespace mmr {
 
@@ -65,22 +62,20 @@ __global__ void __launch_bounds__(256) fft_pass_kernel(const PassArgs a) {
     int lgB = 0;
     while ((1 << lgB) < B) ++lgB;
     const int ls = padded_len(L);
-    const int tid = threadIdx.x, nt = blockDim.x;
 
-    // ---- tile decomposition
-    const bool contiguous = (MODE != PASS_ADJ_COMBINE) && a.inner == 1;
+    // ---- tile decomposition: B consecutive lines (contiguous axis) or B adjacent lines of one
+    //      outer slice (strided axis)
+    const bool contiguous = a.inner == 1;
     const int bufw = fft_buf_words(L, B);
     float2* buf0 = sm;
     float2* buf1 = sm + bufw;
     long long l0 = 0, q0 = 0, o = 0;
-    int coil = 0;
     if (contiguous) {
         l0 = (long long)blockIdx.x * B;
     } else {
         const long long ntq = (a.inner + B - 1) / B;
-        o = (MODE == PASS_ADJ_COMBINE) ? 0 : (long long)blockIdx.x / ntq;
+        o = (long long)blockIdx.x / ntq;
         q0 = ((long long)blockIdx.x % ntq) * B;
-        if (MODE == PASS_ADJ_COMBINE) coil = blockIdx.y;
     }
     auto line_valid = [&](int b) -> bool { return contiguous ? (l0 + b < a.outer) : (q0 + b < a.inner); };
 
@@ -97,110 +92,40 @@ __global__ void __launch_bounds__(256) fft_pass_kernel(const PassArgs a) {
         } else if (contiguous) {
             v = a.in[t + (long long)a.nin * (l0 + b)];
         } else {
-            const long long oo = (MODE == PASS_ADJ_COMBINE) ? coil : o;
-            v = a.in[(q0 + b) + a.inner * (t + (long long)a.nin * oo)];
+            v = a.in[(q0 + b) + a.inner * (t + (long long)a.nin * o)];
         }
         if (a.in_fac) v = cmul(v, a.in_fac[t]);
         return v;
     };
-
-    if (MODE != PASS_ADJ_COMBINE) {
-        // last stage output: natural index n -> output position t = (n - out_start) mod L (crop beyond nout)
-        auto stf = [&](int b, int n, float2 v) {
-            int t = n - a.out_start;
-            t += (t < 0) ? L : 0;
-            if (t >= a.nout || !line_valid(b)) return;
-            v = cscale(v, a.scale);
-            if (a.out_fac) v = cmul(v, a.out_fac[t]);
-            if (contiguous) a.out[t + (long long)a.nout * (l0 + b)] = v;
-            else a.out[(q0 + b) + a.inner * (t + (long long)a.nout * o)] = v;
-        };
-        if (contiguous) run_fft<LC, SIGN, false>(buf0, buf1, a.tw, a.f, B, lgB, ls, ld, stf);
-        else run_fft<LC, SIGN, true>(buf0, buf1, a.tw, a.f, B, lgB, ls, ld, stf);
-        return;
-    }
-
-    // ---- ADJ_COMBINE: crop, deapod, conj(maps) into a staging tile, then a deterministic
-    //      coil sum across the thread-block cluster through distributed shared memory
-    float2* stg = sm + 2 * bufw;
-    auto stc = [&](int b, int n, float2 v) {
+    // last stage output: natural index n -> output position t = (n - out_start) mod L (crop beyond nout)
+    auto stf = [&](int b, int n, float2 v) {
         int t = n - a.out_start;
         t += (t < 0) ? L : 0;
-        if (t >= a.nout) return;
-        float2 r = make_float2(0.f, 0.f);
-        if (line_valid(b)) {
-            r = cscale(v, a.scale);
-            if (a.out_fac) r = cmul(r, a.out_fac[t]);
-            if (a.maps) r = cmulc(r, a.maps[(q0 + b) + a.inner * (t + (long long)a.nout * coil)]);
-        }
-        stg[t * B + b] = r;
+        if (t >= a.nout || !line_valid(b)) return;
+        v = cscale(v, a.scale);
+        if (a.out_fac) v = cmul(v, a.out_fac[t]);
+        if (contiguous) a.out[t + (long long)a.nout * (l0 + b)] = v;
+        else a.out[(q0 + b) + a.inner * (t + (long long)a.nout * o)] = v;
     };
-    run_fft<LC, SIGN, true>(buf0, buf1, a.tw, a.f, B, lgB, ls, ld, stc);
-    cg::cluster_group cl = cg::this_cluster();
-    cl.sync();
-    const int cs = (int)cl.num_blocks();
-    const int rank = (int)cl.block_rank();
-    const int tot = B * a.nout;
-    const int per = (tot + cs - 1) / cs;
-    const int e0 = rank * per, e1 = min(tot, e0 + per);
-    // all ranks' tiles are read with independent DSMEM loads, then summed in rank order
-    const float2* remp[16];
-#pragma unroll
-    for (int r = 0; r < 16; ++r) remp[r] = cl.map_shared_rank(stg, r < cs ? r : 0);
-    for (int idx = e0 + tid; idx < e1; idx += nt) {
-        float2 vals[16];
-#pragma unroll
-        for (int r = 0; r < 16; ++r) vals[r] = r < cs ? remp[r][idx] : make_float2(0.f, 0.f);
-        float2 sum = vals[0];
-#pragma unroll
-        for (int r = 1; r < 16; ++r) sum = cadd(sum, vals[r]);
-        const int t = idx / B, b = idx - t * B;
-        if (q0 + b < a.inner) {
-            float2* dst = a.out + (q0 + b) + a.inner * (long long)t;
-            *dst = a.accumulate ? cadd(*dst, sum) : sum;
-        }
-    }
-    cl.sync();
+    if (contiguous) run_fft<LC, SIGN, false>(buf0, buf1, a.tw, a.f, B, lgB, ls, ld, stf);
+    else run_fft<LC, SIGN, true>(buf0, buf1, a.tw, a.f, B, lgB, ls, ld, stf);
 }
 
 template <int MODE, int SIGN, int LC>
 static void launch_mode(const PassArgs& a, cudaStream_t st) {
-    const size_t smem = (size_t)(2 * fft_buf_words(a.L, a.B) + (MODE == PASS_ADJ_COMBINE ? a.B * a.L : 0)) *
-                        sizeof(float2);
+    const size_t smem = (size_t)2 * fft_buf_words(a.L, a.B) * sizeof(float2);
     auto kern = fft_pass_kernel<MODE, SIGN, LC>;
     static bool attr_done = false;   // one per instantiation
     if (!attr_done) {
         MMR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024));
-        if (MODE == PASS_ADJ_COMBINE)
-            MMR_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
         attr_done = true;
     }
-    const bool contiguous = (MODE != PASS_ADJ_COMBINE) && a.inner == 1;
-    long long nblk;
-    if (contiguous) nblk = (a.outer + a.B - 1) / a.B;
-    else nblk = ((a.inner + a.B - 1) / a.B) * ((MODE == PASS_ADJ_COMBINE) ? 1 : a.outer);
+    const bool contiguous = a.inner == 1;
+    const long long nblk = contiguous ? (a.outer + a.B - 1) / a.B : ((a.inner + a.B - 1) / a.B) * a.outer;
     MMR_REQUIRE(nblk < (1LL << 31), "FFT pass grid too large");
     if (nblk == 0) return;
-    cudaLaunchConfig_t cfg = {};
-    cudaLaunchAttribute attr[1];
-    cfg.blockDim = dim3(256);
-    cfg.dynamicSmemBytes = smem;
-    cfg.stream = st;
-    if (MODE == PASS_ADJ_COMBINE) {
-        const int cs = (int)a.outer;     // coils in the cluster
-        cfg.gridDim = dim3((unsigned)nblk, (unsigned)cs);
-        attr[0].id = cudaLaunchAttributeClusterDimension;
-        attr[0].val.clusterDim.x = 1;
-        attr[0].val.clusterDim.y = cs;
-        attr[0].val.clusterDim.z = 1;
-        cfg.attrs = attr;
-        cfg.numAttrs = 1;
-    } else {
-        cfg.gridDim = dim3((unsigned)nblk);
-        cfg.numAttrs = 0;
-    }
-    MMR_CUDA(cudaLaunchKernelEx(&cfg, kern, a));
-    note_launch();
+    kern<<<(unsigned)nblk, 256, smem, st>>>(a);
+    check_launch("fft_pass_kernel");
 }
 
 template <int LC>
@@ -208,19 +133,16 @@ static void launch_len(int mode, const PassArgs& a, cudaStream_t st) {
     static_assert(LC == 0 || fft_has_cplan(LC), "no compile-time plan");
     if (a.sign < 0) {
         if (mode == PASS_PLAIN) launch_mode<PASS_PLAIN, -1, LC>(a, st);
-        else if (mode == PASS_FWD_IMG) launch_mode<PASS_FWD_IMG, -1, LC>(a, st);
-        else launch_mode<PASS_ADJ_COMBINE, -1, LC>(a, st);
+        else launch_mode<PASS_FWD_IMG, -1, LC>(a, st);
     } else {
         if (mode == PASS_PLAIN) launch_mode<PASS_PLAIN, 1, LC>(a, st);
-        else if (mode == PASS_FWD_IMG) launch_mode<PASS_FWD_IMG, 1, LC>(a, st);
-        else launch_mode<PASS_ADJ_COMBINE, 1, LC>(a, st);
+        else launch_mode<PASS_FWD_IMG, 1, LC>(a, st);
     }
 }
 
 void launch_fft_pass(int mode, const PassArgs& a, cudaStream_t st) {
     MMR_REQUIRE(a.nin <= a.L && a.nout <= a.L && a.nin > 0 && a.nout > 0, "bad FFT pass extents");
     MMR_REQUIRE(a.B >= 1 && (a.B & (a.B - 1)) == 0, "lines per block must be a power of two");
-    if (mode == PASS_ADJ_COMBINE) MMR_REQUIRE(a.outer >= 1 && a.outer <= 16, "cluster coil count must be 1..16");
     switch (a.L) {
         case 512: launch_len<512>(mode, a, st); break;
         case 384: launch_len<384>(mode, a, st); break;

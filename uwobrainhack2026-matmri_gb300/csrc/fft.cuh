@@ -12,7 +12,6 @@
 // oversampled grid used by the gridding kernels.
 #pragma once
 
-#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include "common.h"
@@ -32,14 +31,13 @@ const float2* fft_twiddles(int L);          // device table e^{-2 pi i m / L}, m
 
 enum PassMode : int {
     PASS_PLAIN = 0,     // value = in[...] * in_fac[t]
-    PASS_FWD_IMG = 1,   // value = img[t, line % lpc] * maps[t, c0*lpc + line] * in_fac[t]
-    PASS_ADJ_COMBINE = 2 // out[q, t] (+)= sum_c fft(...)[t] * out_fac[t] * conj(maps[q, t, c])
+    PASS_FWD_IMG = 1    // value = img[t, line % lpc] * maps[t, c0*lpc + line] * in_fac[t]
 };
 
 struct PassArgs {
     const float2* in = nullptr;
     float2* out = nullptr;
-    const float2* maps = nullptr;   // FWD_IMG / ADJ_COMBINE
+    const float2* maps = nullptr;   // FWD_IMG
     const float2* in_fac = nullptr; // per input position (nullable)
     const float2* out_fac = nullptr;// per output position (nullable)
     const float2* tw = nullptr;
@@ -53,7 +51,6 @@ struct PassArgs {
     int sign = -1;                  // -1: e^{-i} (fft), +1: e^{+i} (ifft)
     float scale = 1.f;
     int B = 1;                      // lines per block (power of two)
-    int accumulate = 0;             // ADJ_COMBINE: out += (1) or out = (0)
     FftFactors f;
 };
 
@@ -363,7 +360,7 @@ __device__ __forceinline__ void run_fft(float2* a, float2* b, const float2* tw, 
     else cstages<LC, 0, SIGN, TR>(a, b, tw, B, lgB, ls, ld, stf);
 }
 
-// Launch a pass (host). `cluster` > 1 only for PASS_ADJ_COMBINE.
+// Launch a pass (host).
 void launch_fft_pass(int mode, const PassArgs& a, cudaStream_t st);
 
 }  // namespace mmr

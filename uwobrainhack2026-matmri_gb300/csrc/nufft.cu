@@ -1112,6 +1112,19 @@ size_t nufft_grid_to_img_scratch(const NufftPlan& p, long long nb) {
     return need + need2;
 }
 
+// out (+)= sum_c conj(maps_c) .* img_c over nb per-coil images of n voxels (the rcvrOp adjoint,
+// rcvrOp.m:144-157, after the per-coil nufftOp adjoint), summed in coil order: deterministic.
+__global__ void __launch_bounds__(256) coil_combine_kernel(const float2* __restrict__ img,
+                                                           const float2* __restrict__ maps, float2* __restrict__ out,
+                                                           long long n, int nb, int accumulate, const int* active) {
+    if (active && *active) return;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+        float2 s = make_float2(0.f, 0.f);
+        for (int c = 0; c < nb; ++c) s = cadd(s, cmulc(img[i + n * c], maps[i + n * c]));
+        out[i] = accumulate ? cadd(out[i], s) : s;
+    }
+}
+
 void nufft_grid_to_img(NufftPlan& p, const float2* grid, const float2* maps, float2* out, long long nb,
                        bool accumulate, cudaStream_t st, const int* active, float2* scratch) {
     long long ext[3] = {p.G[0], p.G[1], p.G[2]};
@@ -1120,6 +1133,12 @@ void nufft_grid_to_img(NufftPlan& p, const float2* grid, const float2* maps, flo
         p.s_tmp.ensure(nufft_grid_to_img_scratch(p, nb) * sizeof(float2));
         tmp = p.s_tmp.as<float2>();
     }
+    // with maps, the last pass writes the per-coil images, then one kernel weights and sums them
+    float2* per_coil = nullptr;
+    if (maps) {
+        p.s_coil.ensure((size_t)p.Ntot * nb * sizeof(float2));
+        per_coil = p.s_coil.as<float2>();
+    }
     const float2* src = grid;
     for (int ax = 0; ax < p.nd; ++ax) {
         PassArgs a = base_pass(p, ax, -1);
@@ -1127,6 +1146,7 @@ void nufft_grid_to_img(NufftPlan& p, const float2* grid, const float2* maps, flo
         for (int k = 0; k < ax; ++k) inner *= p.N[k];
         for (int k = ax + 1; k < 3; ++k) outer *= ext[k];
         a.inner = inner;
+        a.outer = outer;
         a.nin = p.G[ax];
         a.in_start = p.G[ax] / 2;
         a.nout = p.N[ax];
@@ -1135,26 +1155,21 @@ void nufft_grid_to_img(NufftPlan& p, const float2* grid, const float2* maps, flo
         a.active = active;
         const bool last = ax == p.nd - 1;
         float2* dst;
-        if (last) dst = out;
+        if (last) dst = maps ? per_coil : out;
         else if (ax == 0) dst = tmp;
         else dst = tmp + (size_t)p.N[0] * p.G[1] * p.G[2] * nb;
         a.in = src;
         a.out = dst;
-        int mode = PASS_PLAIN;
-        if (last && maps) {
-            mode = PASS_ADJ_COMBINE;
-            a.maps = maps;
-            a.outer = nb;          // coils summed by the cluster
-            a.accumulate = accumulate ? 1 : 0;
-            a.B = pow2_floor(std::max(1, (int)std::min<long long>(std::min<long long>(p.fft_lines, inner), 4096 / a.L)));
-            if (inner == 1) a.B = 1;
-        } else {
-            a.outer = outer;
-        }
         prof_mark(last ? 4 : 3, st);
-        launch_fft_pass(mode, a, st);
+        launch_fft_pass(PASS_PLAIN, a, st);
         ext[ax] = p.N[ax];
         src = dst;
+    }
+    if (maps) {
+        const long long n = p.Ntot;
+        const unsigned blocks = (unsigned)std::min<long long>(cdiv(n, 256), (long long)device_sm_count() * 8);
+        coil_combine_kernel<<<blocks, 256, 0, st>>>(per_coil, maps, out, n, (int)nb, accumulate ? 1 : 0, active);
+        check_launch("coil_combine_kernel");
     }
 }
 

@@ -57,6 +57,7 @@ struct NufftPlan {
     int fft_lines = 8;            // lines per CTA in the FFT passes (autotuned, power of two)
     // scratch
     DevBuf s_tmp, s_grid, s_grid2;
+    DevBuf s_coil;                // per-coil images before the coil sum
     Staged st_in, st_out;
     // TMA descriptor cache for the interp kernel (keyed by grid buffer / batch)
     CUtensorMap tmap;

@@ -67,7 +67,7 @@ int sense_chunk(const SenseOp& a) {
     if (!a.rcvr) return 1;
     int cc = a.coil_chunk > 0 ? a.coil_chunk : 8;
     cc = (int)std::min<long long>(cc, a.C);
-    return std::max(1, std::min(cc, 16));
+    return std::max(1, std::min(cc, 32));
 }
 
 void sense_set_weights(SenseOp& a, const float* cgW, bool cgW_per_coil) {
@@ -423,7 +423,7 @@ extern "C" int mmr_sense_set_tuning(mmr_sense* h, const mmr_tuning* t) {
     return guarded([&] {
         MMR_REQUIRE(h && t, "NULL argument");
         SenseOp& a = h->a;
-        MMR_REQUIRE(t->coil_chunk >= 0 && t->coil_chunk <= 16, "coil_chunk must be 0..16");
+        MMR_REQUIRE(t->coil_chunk >= 0 && t->coil_chunk <= 32, "coil_chunk must be 0..32");
         MMR_REQUIRE(t->coil_group == 0 || t->coil_group == 1 || t->coil_group == 2 || t->coil_group == 4 ||
                         t->coil_group == 8, "coil_group must be 1, 2, 4 or 8");
         MMR_REQUIRE(t->item == 0 || t->item >= 8, "item must be >= 8");

@@ -27,8 +27,8 @@ import numpy as np
 from . import _lib
 
 SPACE = {
-    "coil_chunk": [4, 8, 16],
-    "tile": [16, 32],
+    "coil_chunk": [4, 8, 16, 32],
+    "tile": [16, 32, 64],
     "coil_group": [2, 4, 8],
     "item": [32, 64, 128, 256],
     "fft_lines": [4, 8, 16],

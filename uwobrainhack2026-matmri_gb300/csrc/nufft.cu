@@ -686,7 +686,7 @@ __host__ __device__ __forceinline__ int gn_area(int T, int W) {
 // `chunk`: items are built that way) are interpolated from the staged input region, weighted,
 // and spread into the (sub)tile's accumulators, which alias the region.
 template <int W>
-__global__ void __launch_bounds__(256) gridnorm2d_binned(const float2* __restrict__ gin, float2* __restrict__ gout,
+__global__ void __launch_bounds__(256, 5) gridnorm2d_binned(const float2* __restrict__ gin, float2* __restrict__ gout,
                                                          const Bin2DArgs a, const __grid_constant__ CUtensorMap tmap) {
     using TM = TapMap<W>;
     extern __shared__ float4 sm4[];

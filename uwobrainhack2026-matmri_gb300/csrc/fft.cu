@@ -80,6 +80,12 @@ __global__ void __launch_bounds__(256) fft_pass_kernel(const PassArgs a) {
     auto line_valid = [&](int b) -> bool { return contiguous ? (l0 + b < a.outer) : (q0 + b < a.inner); };
 
     // first stage input: natural index n <- input position t = (n - in_start) mod L (zero padding beyond nin)
+    auto line_in = [&](int b) -> float2 {
+        return a.in_line ? a.in_line[(l0 + b) % a.lpc] : make_float2(1.f, 0.f);
+    };
+    auto line_out = [&](int b) -> float2 {
+        return a.out_line ? a.out_line[q0 + b] : make_float2(1.f, 0.f);
+    };
     auto ld = [&](int b, int n) -> float2 {
         int t = n - a.in_start;
         t += (t < 0) ? L : 0;
@@ -95,6 +101,7 @@ __global__ void __launch_bounds__(256) fft_pass_kernel(const PassArgs a) {
             v = a.in[(q0 + b) + a.inner * (t + (long long)a.nin * o)];
         }
         if (a.in_fac) v = cmul(v, a.in_fac[t]);
+        if (a.in_line) v = cmul(v, line_in(b));
         return v;
     };
     // last stage output: natural index n -> output position t = (n - out_start) mod L (crop beyond nout)
@@ -104,6 +111,7 @@ __global__ void __launch_bounds__(256) fft_pass_kernel(const PassArgs a) {
         if (t >= a.nout || !line_valid(b)) return;
         v = cscale(v, a.scale);
         if (a.out_fac) v = cmul(v, a.out_fac[t]);
+        if (a.out_line) v = cmul(v, line_out(b));
         if (contiguous) a.out[t + (long long)a.nout * (l0 + b)] = v;
         else a.out[(q0 + b) + a.inner * (t + (long long)a.nout * o)] = v;
     };
@@ -141,6 +149,8 @@ static void launch_len(int mode, const PassArgs& a, cudaStream_t st) {
 }
 
 void launch_fft_pass(int mode, const PassArgs& a, cudaStream_t st) {
+    MMR_REQUIRE(!a.in_line || (a.inner == 1 && a.lpc >= 1), "per-line input factors need a contiguous pass");
+    MMR_REQUIRE(!a.out_line || a.inner > 1, "per-line output factors need a strided pass");
     MMR_REQUIRE(a.nin <= a.L && a.nout <= a.L && a.nin > 0 && a.nout > 0, "bad FFT pass extents");
     MMR_REQUIRE(a.B >= 1 && (a.B & (a.B - 1)) == 0, "lines per block must be a power of two");
     switch (a.L) {

@@ -40,11 +40,13 @@ struct PassArgs {
     const float2* maps = nullptr;   // FWD_IMG
     const float2* in_fac = nullptr; // per input position (nullable)
     const float2* out_fac = nullptr;// per output position (nullable)
+    const float2* in_line = nullptr;  // per input line, indexed by line % lpc (contiguous passes; nullable)
+    const float2* out_line = nullptr; // per output line, indexed by the inner index (strided passes; nullable)
     const float2* tw = nullptr;
     const int* active = nullptr;    // solver "finished" flag: skip when *active != 0
     long long inner = 1;            // product of dims before the axis
     long long outer = 1;            // product of dims after the axis (lines = inner*outer)
-    long long lpc = 1;              // FWD_IMG: lines per coil (image lines)
+    long long lpc = 1;              // FWD_IMG / in_line: lines per coil (image lines)
     int L = 0;
     int nin = 0, in_start = 0;
     int nout = 0, out_start = 0;

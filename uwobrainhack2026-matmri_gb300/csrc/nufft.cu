@@ -28,6 +28,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cudaTypedefs.h>
+#include <complex>
 #include <functional>
 
 #include "nufft.cuh"
@@ -114,6 +115,7 @@ void nufft_plan_build(NufftPlan& p, const mmr_nufft_desc& d) {
     for (auto& v : kern) v = v / ksum * (double)(Nk - 1) / p.W;
 
     // deapodisation (171-181) and the fftShiftArray constant exp(+-i pi N/2)
+    std::vector<std::complex<double>> fac64[3];
     for (int k = 0; k < p.nd; ++k) {
         const int n = p.N[k], g = p.G[k];
         std::vector<double> c(n);
@@ -131,8 +133,10 @@ void nufft_plan_build(NufftPlan& p, const mmr_nufft_desc& d) {
         const double cm = c[imin], sc = std::sqrt((double)g / n);
         const double ph = M_PI * n / 2.0;
         std::vector<float2> ff(n), fa(n);
+        fac64[k].resize(n);
         for (int i = 0; i < n; ++i) {
             const double v = c[i] / cm * sc;
+            fac64[k][i] = {v * std::cos(ph), v * std::sin(ph)};
             ff[i] = make_float2((float)(v * std::cos(ph)), (float)(v * std::sin(ph)));
             fa[i] = make_float2((float)(v * std::cos(ph)), (float)(-v * std::sin(ph)));
         }
@@ -140,6 +144,23 @@ void nufft_plan_build(NufftPlan& p, const mmr_nufft_desc& d) {
         p.d_adj_fac[k].upload(fa);
         p.ff[k] = fft_factorize(g);
         p.tw[k] = fft_twiddles(g);
+    }
+    if (p.nd > 1) {
+        // per-line products in FP64, rounded once: forward over axes 1.., adjoint over axes ..nd-2
+        const long long nf = (long long)p.N[1] * p.N[2], na = (long long)p.N[0] * (p.nd > 2 ? p.N[1] : 1);
+        std::vector<float2> fl((size_t)nf), al((size_t)na);
+        for (long long l = 0; l < nf; ++l) {
+            std::complex<double> f = fac64[1][l % p.N[1]];
+            if (p.nd > 2) f *= fac64[2][l / p.N[1]];
+            fl[(size_t)l] = make_float2((float)f.real(), (float)f.imag());
+        }
+        for (long long q = 0; q < na; ++q) {
+            std::complex<double> f = std::conj(fac64[0][q % p.N[0]]);
+            if (p.nd > 2) f *= std::conj(fac64[1][q / p.N[0]]);
+            al[(size_t)q] = make_float2((float)f.real(), (float)f.imag());
+        }
+        p.d_fwd_line.upload(fl);
+        p.d_adj_line.upload(al);
     }
 
     // per-sample base cells and tap weights (216-238)
@@ -1084,7 +1105,12 @@ void nufft_img_to_grid(NufftPlan& p, const float2* x, const float2* maps, float2
         a.in_start = p.G[ax] - p.N[ax] / 2;
         a.nout = p.G[ax];
         a.out_start = p.G[ax] / 2;
-        a.in_fac = p.d_fwd_fac[ax].as<float2>();
+        // axis 0 applies its own factor per point and the others' per line; later axes none
+        a.in_fac = ax == 0 ? p.d_fwd_fac[0].as<float2>() : nullptr;
+        if (ax == 0 && p.nd > 1) {
+            a.in_line = p.d_fwd_line.as<float2>();
+            a.lpc = (long long)p.N[1] * p.N[2];
+        }
         a.active = active;
         float2* dst;
         if (ax == p.nd - 1) dst = grid;
@@ -1151,9 +1177,11 @@ void nufft_grid_to_img(NufftPlan& p, const float2* grid, const float2* maps, flo
         a.in_start = p.G[ax] / 2;
         a.nout = p.N[ax];
         a.out_start = p.G[ax] - p.N[ax] / 2;
-        a.out_fac = p.d_adj_fac[ax].as<float2>();
-        a.active = active;
+        // the last axis applies its own factor per point and the others' per line; earlier axes none
         const bool last = ax == p.nd - 1;
+        a.out_fac = last ? p.d_adj_fac[ax].as<float2>() : nullptr;
+        if (last && p.nd > 1) a.out_line = p.d_adj_line.as<float2>();
+        a.active = active;
         float2* dst;
         if (last) dst = maps ? per_coil : out;
         else if (ax == 0) dst = tmp;

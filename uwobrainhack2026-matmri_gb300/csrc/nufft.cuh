@@ -44,6 +44,10 @@ struct NufftPlan {
     bool has_dcf = false;
     int dcf_version = 0;
     DevBuf d_fwd_fac[3], d_adj_fac[3];   // float2 [N_d]: deapod * exp(+-i pi N_d / 2)
+    // the other axes' factors folded into one per transform line (nd > 1): the first
+    // image->grid pass multiplies line (j, k) by fwd_1[j] fwd_2[k], the last grid->image pass
+    // line (i, j) by adj_0[i] adj_1[j]; the passes in between apply none
+    DevBuf d_fwd_line, d_adj_line;
     FftFactors ff[3];
     const float2* tw[3] = {nullptr, nullptr, nullptr};
     BinLists bins;                // valid when use_bins

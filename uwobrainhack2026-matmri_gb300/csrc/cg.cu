@@ -45,13 +45,14 @@ struct CgWorkspace {
     DevBuf x, p, res, Ap, b, tmp, tik, gt, state, hist, noise, nimg;
     Staged sb, sxo;
     // graph cache
-    cudaGraphExec_t g_norm = nullptr, g_expl = nullptr;
-    int k_norm = 0, k_expl = 0;   // kernel nodes per graph
+    cudaGraphExec_t g_norm = nullptr, g_expl = nullptr, g_run = nullptr;
+    int k_norm = 0, k_expl = 0, k_run = 0;   // kernel nodes per graph
     const void* key[8] = {nullptr};
     long long keyv[4] = {0};
     ~CgWorkspace() {
         if (g_norm) cudaGraphExecDestroy(g_norm);
         if (g_expl) cudaGraphExecDestroy(g_expl);
+        if (g_run) cudaGraphExecDestroy(g_run);
     }
 };
 
@@ -331,6 +332,15 @@ static cudaGraphExec_t capture_iter(SenseOp& a, CgWorkspace& w, bool expl, bool 
     return capture(a.stream, [&] { iter_body(a, w, expl, has_tik, has_gt, a.stream); }, kernels);
 }
 
+// Plain iterations per run graph: consecutive iterations captured back to back in one graph,
+// so the kernels at iteration boundaries overlap like those inside an iteration.
+constexpr int kRunIters = 8;
+static cudaGraphExec_t capture_run(SenseOp& a, CgWorkspace& w, bool has_tik, bool has_gt, int& kernels) {
+    return capture(a.stream, [&] {
+        for (int i = 0; i < kRunIters; ++i) iter_body(a, w, false, has_tik, has_gt, a.stream);
+    }, kernels);
+}
+
 // Instantiates `gr` (destroyed here) and counts its kernel nodes.
 static cudaGraphExec_t instantiate_counted(cudaGraph_t gr, int& kernels) {
     size_t nn = 0;
@@ -523,10 +533,12 @@ static void cg_solve(SenseOp& a, const void* b_user, const void* x0_user, const 
     if (!same) {
         if (w.g_norm) cudaGraphExecDestroy(w.g_norm);
         if (w.g_expl) cudaGraphExecDestroy(w.g_expl);
-        w.g_norm = w.g_expl = nullptr;
+        if (w.g_run) cudaGraphExecDestroy(w.g_run);
+        w.g_norm = w.g_expl = w.g_run = nullptr;
         // the eager initial residual has sized every scratch buffer before capture
         w.g_norm = capture_iter(a, w, false, run.has_tik, run.has_gt, w.k_norm);
         w.g_expl = capture_iter(a, w, true, run.has_tik, run.has_gt, w.k_expl);
+        w.g_run = capture_run(a, w, run.has_tik, run.has_gt, w.k_run);
         for (int i = 0; i < 8; ++i) w.key[i] = key[i];
         for (int i = 0; i < 4; ++i) w.keyv[i] = keyv[i];
     }
@@ -534,10 +546,20 @@ static void cg_solve(SenseOp& a, const void* b_user, const void* x0_user, const 
     int it = 0;
     while (it < run.limit) {
         const int end = std::min(run.limit, it + poll);
-        for (; it < end; ++it) {
+        while (it < end) {
+            // kRunIters plain iterations in one launch when none of them needs the explicit residual
+            bool plain_run = it + kRunIters <= end;
+            for (int j = it; j < it + kRunIters && plain_run; ++j) plain_run = j % run.expResN != 0;
+            if (plain_run) {
+                MMR_CUDA(cudaGraphLaunch(w.g_run, st));
+                add_launches(w.k_run);
+                it += kRunIters;
+                continue;
+            }
             const bool ex = it % run.expResN == 0;
             MMR_CUDA(cudaGraphLaunch(ex ? w.g_expl : w.g_norm, st));
             add_launches(ex ? w.k_expl : w.k_norm);
+            ++it;
         }
         int fin = 0;
         MMR_CUDA(cudaMemcpyAsync(&fin, &sp->finished, sizeof(int), cudaMemcpyDeviceToHost, st));

@@ -80,6 +80,36 @@ inline void check_launch(const char* what) {
     note_launch();
 }
 
+// ------------------------------------------------ programmatic dependent launch ----
+// A kernel launched with launch_dependent() may be scheduled while the kernel before it
+// on the stream is still finishing (its CTAs fill the SMs that the tail frees).  Every
+// such kernel calls pdl_wait() before it touches global memory, which returns once the
+// previous grid has completed and its writes are visible; pdl_trigger() then lets the
+// next kernel start launching once all of this grid's CTAs are running.  Both are
+// no-ops in a kernel launched the ordinary way.
+__device__ __forceinline__ void pdl_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void pdl_trigger() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+template <class... KArgs, class... Args>
+void launch_dependent(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t st, Args&&... args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
+    if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        MMR_THROW(MMR_ERR_CUDA, "launch failed: %s", cudaGetErrorString(e));
+    }
+    note_launch();
+}
+
 // ----------------------------------------------------------- device buffer ----
 struct DevBuf {
     void* p = nullptr;

@@ -57,6 +57,8 @@ template <int MODE, int SIGN, int LC>
 __global__ void __launch_bounds__(256) fft_pass_kernel(const PassArgs a) {
     extern __shared__ float4 sm4[];
     float2* sm = reinterpret_cast<float2*>(sm4);
+    pdl_wait();
+    pdl_trigger();
     if (a.active && *a.active) return;
     const int L = LC ? LC : a.L, B = a.B;
     int lgB = 0;
@@ -132,8 +134,7 @@ static void launch_mode(const PassArgs& a, cudaStream_t st) {
     const long long nblk = contiguous ? (a.outer + a.B - 1) / a.B : ((a.inner + a.B - 1) / a.B) * a.outer;
     MMR_REQUIRE(nblk < (1LL << 31), "FFT pass grid too large");
     if (nblk == 0) return;
-    kern<<<(unsigned)nblk, 256, smem, st>>>(a);
-    check_launch("fft_pass_kernel");
+    launch_dependent(kern, dim3((unsigned)nblk), dim3(256), smem, st, a);
 }
 
 template <int LC>

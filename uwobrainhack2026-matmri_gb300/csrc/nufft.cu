@@ -599,6 +599,8 @@ __device__ __forceinline__ void flush_tile(const float* acc, float2* __restrict_
 // Zeroes the shared leaf tiles (block (k, c): tile k of plane c) before their items add into them.
 __global__ void __launch_bounds__(256) zero_shared_tiles(float2* __restrict__ out, const int2* __restrict__ tiles,
                                                          int G1, int G2, const int* active) {
+    pdl_wait();
+    pdl_trigger();
     if (active && *active) return;
     const int2 t = tiles[blockIdx.x];
     const int u0 = t.x & 0xffff, v0 = t.x >> 16, T = t.y;
@@ -612,9 +614,8 @@ __global__ void __launch_bounds__(256) zero_shared_tiles(float2* __restrict__ ou
 static void zero_shared(NufftPlan& p, float2* out, long long nb, cudaStream_t st, const int* active) {
     const BinLists& b = p.bins;
     if (b.n_heavy == 0) return;
-    zero_shared_tiles<<<dim3((unsigned)b.n_heavy, (unsigned)nb), 256, 0, st>>>(out, b.heavy.as<int2>(), p.G[0],
-                                                                             p.G[1], active);
-    check_launch("zero_shared_tiles");
+    launch_dependent(zero_shared_tiles, dim3((unsigned)b.n_heavy, (unsigned)nb), dim3(256), 0, st, out,
+                     b.heavy.as<int2>(), p.G[0], p.G[1], active);
 }
 
 // Zeroes n floats (n a multiple of 4).
@@ -711,6 +712,8 @@ __global__ void __launch_bounds__(256, 5) gridnorm2d_binned(const float2* __rest
                                                          const Bin2DArgs a, const __grid_constant__ CUtensorMap tmap) {
     using TM = TapMap<W>;
     extern __shared__ float4 sm4[];
+    pdl_wait();
+    pdl_trigger();
     if (a.active && *a.active) return;
     const int4 item = a.items[blockIdx.x];
     const int T = item.w & 255, R = T + 2 * W; // this item's (sub)tile and region sides
@@ -1058,9 +1061,8 @@ void nufft_grid_normal(NufftPlan& p, const float2* gin, float2* gout, long long 
     zero_shared(p, gout, nb, st, active);
     MMR_W_DISPATCH(p.W, {
         set_smem(gridnorm2d_binned<KW>, smem);
-        gridnorm2d_binned<KW><<<gridDim, 256, smem, st>>>(gin, gout, a, g_norm_map);
+        launch_dependent(gridnorm2d_binned<KW>, gridDim, dim3(256), smem, st, gin, gout, a, g_norm_map);
     });
-    check_launch("gridnorm2d_binned");
 }
 
 // ------------------------------------------------------------- FFT pipelines --
@@ -1143,6 +1145,8 @@ size_t nufft_grid_to_img_scratch(const NufftPlan& p, long long nb) {
 __global__ void __launch_bounds__(256) coil_combine_kernel(const float2* __restrict__ img,
                                                            const float2* __restrict__ maps, float2* __restrict__ out,
                                                            long long n, int nb, int accumulate, const int* active) {
+    pdl_wait();
+    pdl_trigger();
     if (active && *active) return;
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         float2 s = make_float2(0.f, 0.f);
@@ -1196,8 +1200,8 @@ void nufft_grid_to_img(NufftPlan& p, const float2* grid, const float2* maps, flo
     if (maps) {
         const long long n = p.Ntot;
         const unsigned blocks = (unsigned)std::min<long long>(cdiv(n, 256), (long long)device_sm_count() * 8);
-        coil_combine_kernel<<<blocks, 256, 0, st>>>(per_coil, maps, out, n, (int)nb, accumulate ? 1 : 0, active);
-        check_launch("coil_combine_kernel");
+        launch_dependent(coil_combine_kernel, dim3(blocks), dim3(256), 0, st, per_coil, maps, out, n, (int)nb,
+                         accumulate ? 1 : 0, active);
     }
 }
 

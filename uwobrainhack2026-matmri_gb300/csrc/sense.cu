@@ -57,6 +57,8 @@ __global__ void weight_kernel(const float2* __restrict__ y, const float* __restr
 
 __global__ void axpy_real_kernel(float2* __restrict__ y, const float2* __restrict__ x, float a, long long n,
                                  const int* active) {
+    pdl_wait();
+    pdl_trigger();
     if (active && *active) return;
     const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
@@ -240,9 +242,8 @@ void sense_normal(SenseOp& a, const float2* x, float2* y, cudaStream_t st, const
     }
     prof_mark(-1, st);
     if (a.tikreg != 0) {
-        axpy_real_kernel<<<(unsigned)cdiv(a.Nimg, 256), 256, 0, st>>>(y, x, (float)(a.tikreg * a.tikreg), a.Nimg,
-                                                                    active);
-        check_launch("tikreg");
+        launch_dependent(axpy_real_kernel, dim3((unsigned)cdiv(a.Nimg, 256)), dim3(256), 0, st, y, x,
+                         (float)(a.tikreg * a.tikreg), a.Nimg, active);
     }
 }
 

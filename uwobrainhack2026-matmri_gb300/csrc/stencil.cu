@@ -71,6 +71,8 @@ __global__ void __launch_bounds__(256) stencil2d_kernel(const float2* __restrict
     constexpr int RX = TX + 2 * H, RY = TY + 2 * H;
     extern __shared__ float4 sm4[];
     float2* reg = reinterpret_cast<float2*>(sm4);   // [CGS][RY][RX]
+    pdl_wait();
+    pdl_trigger();
     if (active && *active) return;
     const int u0 = blockIdx.x * TX, v0 = blockIdx.y * TY, c0 = blockIdx.z * CGS;
     // stage the tile + halo (periodic wrap), one warp per (coil, row)
@@ -140,9 +142,8 @@ static void launch_stencil(const NufftPlan& p, const float2* gin, float2* gout, 
     const size_t smem = (size_t)CGS * RX * RY * sizeof(float2);
     MMR_CUDA(cudaFuncSetAttribute(stencil2d_kernel<W, CGS>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     dim3 grid((unsigned)cdiv(p.G[0], 64), (unsigned)cdiv(p.G[1], 16), (unsigned)cdiv(nb, CGS));
-    stencil2d_kernel<W, CGS><<<grid, 256, smem, st>>>(gin, gout, p.d_stencil.as<float>(), p.G[0], p.G[1], nb,
-                                                       active);
-    check_launch("stencil2d");
+    launch_dependent(stencil2d_kernel<W, CGS>, grid, dim3(256), smem, st, gin, gout, p.d_stencil.as<float>(), p.G[0],
+                     p.G[1], nb, active);
 }
 
 template <int W>

@@ -274,7 +274,7 @@ __global__ void norm2_kernel(const float2* __restrict__ v, long long n, double* 
 
 static unsigned red_grid(long long n) {
     const long long b = cdiv(n, 256);
-    return (unsigned)std::max<long long>(1, std::min<long long>(b, 2LL * device_sm_count()));
+    return (unsigned)std::max<long long>(1, std::min<long long>(b, (long long)device_sm_count()));
 }
 
 static bool isset(double v) { return !std::isnan(v); }

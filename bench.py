@@ -572,7 +572,8 @@ def stage_bytes(cc, N, G, M, W, stencil):
         cc * half + cc * grid,               # 1: second-axis FFT (G x N -> G x G per coil)
         2 * cc * grid + sten,                # 2: gridding normal op (grid in, grid out; + stencil weights once)
         cc * grid + cc * half,               # 3: first-axis FFT + crop (G x G -> N x G per coil)
-        cc * half + cc * img + 2 * img,      # 4: second-axis FFT + crop + deapod + conj maps + coil sum
+        cc * half + 3 * cc * img + 2 * img,  # 4: second-axis FFT + crop + deapod per coil (writes N x N per coil),
+                                             #    then conj maps x per-coil images summed over coils
     ]
 
 

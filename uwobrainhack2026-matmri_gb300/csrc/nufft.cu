@@ -331,6 +331,12 @@ void nufft_build_bins(NufftPlan& p, int Treq, int chunk) {
         }
     };
     for (int t = 0; t < ntile; ++t) split((t % b.ntx) * T, (t / b.ntx) * T, T, tiles_s[t]);
+    // costliest items first (about 100 instructions per entry and coil, 10 per cell and coil), so
+    // that the long ones start in the first wave of a launch instead of trailing in the last
+    std::stable_sort(items.begin(), items.end(), [](const int4& x, const int4& y) {
+        const long long tx = x.w & 255, ty = y.w & 255;
+        return 100LL * (x.z - x.y) + 10 * tx * tx > 100LL * (y.z - y.y) + 10 * ty * ty;
+    });
     b.heavy.upload(heavy);
     b.n_heavy = (int)heavy.size();
     b.pad_s.upload(ps);
@@ -495,6 +501,7 @@ struct Bin2DArgs {
     int cg;
     int use_tma;
     int chunk;               // max entries per phase batch (sval capacity)
+    int n_items;             // work items in the list
     const int* active;
 };
 
@@ -715,11 +722,14 @@ __global__ void __launch_bounds__(256, 5) gridnorm2d_binned(const float2* __rest
     pdl_wait();
     pdl_trigger();
     if (a.active && *a.active) return;
-    const int4 item = a.items[blockIdx.x];
+    // all coil groups of an item launch together (blockIdx.x); items along y, then z past 65535
+    const long long it = blockIdx.y + (long long)gridDim.y * blockIdx.z;
+    if (it >= a.n_items) return;
+    const int4 item = a.items[it];
     const int T = item.w & 255, R = T + 2 * W; // this item's (sub)tile and region sides
     const bool shared = (item.w >> 8) != 0;    // tile split across several items
     const int u0 = item.x & 0xffff, v0 = item.x >> 16;
-    const int c0 = blockIdx.y * a.cg;
+    const int c0 = blockIdx.x * a.cg;
     const int te1 = min(T, a.G1 - u0), te2 = min(T, a.G2 - v0);
     const int e0 = item.y, ne = item.z - item.y;
     if (ne == 0) {
@@ -947,6 +957,7 @@ static Bin2DArgs bin_args(const NufftPlan& p, bool own, const float* wfac, long 
     a.cg = cg;
     a.use_tma = tma ? 1 : 0;
     a.chunk = b.chunk;
+    a.n_items = own ? b.n_own_items : b.n_pad_items;
     a.active = active;
     return a;
 }
@@ -1057,7 +1068,8 @@ void nufft_grid_normal(NufftPlan& p, const float2* gin, float2* gout, long long 
     }
     const size_t smem = kTmaSmemExtra + ent + (size_t)cg * per_coil;
     Bin2DArgs a = bin_args(p, false, wfac, wfb, nb, cg, true, active);
-    dim3 gridDim((unsigned)p.bins.n_pad_items, (unsigned)cdiv(nb, cg));
+    const long long ny = std::min(p.bins.n_pad_items, 65535);
+    dim3 gridDim((unsigned)cdiv(nb, cg), (unsigned)ny, (unsigned)cdiv(p.bins.n_pad_items, ny));
     zero_shared(p, gout, nb, st, active);
     MMR_W_DISPATCH(p.W, {
         set_smem(gridnorm2d_binned<KW>, smem);

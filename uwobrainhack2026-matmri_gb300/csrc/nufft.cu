@@ -32,6 +32,7 @@
 #include <functional>
 
 #include "nufft.cuh"
+#include "reduce.cuh"
 
 namespace mmr {
 
@@ -1154,21 +1155,38 @@ size_t nufft_grid_to_img_scratch(const NufftPlan& p, long long nb) {
 
 // out (+)= sum_c conj(maps_c) .* img_c over nb per-coil images of n voxels (the rcvrOp adjoint,
 // rcvrOp.m:144-157, after the per-coil nufftOp adjoint), summed in coil order: deterministic.
+// With dacc: the DotEpilogue (out += tik .* dv, then dacc += v' out) in the same pass.
 __global__ void __launch_bounds__(256) coil_combine_kernel(const float2* __restrict__ img,
                                                            const float2* __restrict__ maps, float2* __restrict__ out,
-                                                           long long n, int nb, int accumulate, const int* active) {
+                                                           long long n, int nb, int accumulate, const int* active,
+                                                           const float2* __restrict__ dv,
+                                                           const float* __restrict__ tik, double* dacc) {
     pdl_wait();
     pdl_trigger();
     if (active && *active) return;
+    double d[2] = {0, 0};
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         float2 s = make_float2(0.f, 0.f);
         for (int c = 0; c < nb; ++c) s = cadd(s, cmulc(img[i + n * c], maps[i + n * c]));
-        out[i] = accumulate ? cadd(out[i], s) : s;
+        if (accumulate) s = cadd(out[i], s);
+        if (dacc) {
+            const float2 v = dv[i];
+            if (tik) s = make_float2(s.x + tik[i] * v.x, s.y + tik[i] * v.y);
+            d[0] += (double)v.x * s.x + (double)v.y * s.y;     // re(conj(v) s)
+            d[1] += (double)v.x * s.y - (double)v.y * s.x;     // im(conj(v) s)
+        }
+        out[i] = s;
+    }
+    if (dacc) {
+        double* const dst[2] = {dacc, dacc + 1};
+        block_accumulate<2>(d, dst);
     }
 }
 
 void nufft_grid_to_img(NufftPlan& p, const float2* grid, const float2* maps, float2* out, long long nb,
-                       bool accumulate, cudaStream_t st, const int* active, float2* scratch) {
+                       bool accumulate, cudaStream_t st, const int* active, float2* scratch,
+                       const DotEpilogue* dot) {
+    MMR_REQUIRE(!dot || maps, "the dot epilogue runs in the coil sum");
     long long ext[3] = {p.G[0], p.G[1], p.G[2]};
     float2* tmp = scratch;
     if (p.nd > 1 && !tmp) {
@@ -1213,7 +1231,8 @@ void nufft_grid_to_img(NufftPlan& p, const float2* grid, const float2* maps, flo
         const long long n = p.Ntot;
         const unsigned blocks = (unsigned)std::min<long long>(cdiv(n, 256), (long long)device_sm_count() * 8);
         launch_dependent(coil_combine_kernel, dim3(blocks), dim3(256), 0, st, per_coil, maps, out, n, (int)nb,
-                         accumulate ? 1 : 0, active);
+                         accumulate ? 1 : 0, active, dot ? dot->v : nullptr, dot ? dot->tik : nullptr,
+                         dot ? dot->acc : nullptr);
     }
 }
 

@@ -98,9 +98,16 @@ void nufft_img_to_grid(NufftPlan& p, const float2* x, const float2* maps, float2
 // over the nb coils into out (accumulate: out += ...).
 // `scratch` (optional) replaces the plan's intermediate buffer; it must hold
 // nufft_grid_to_img_scratch(p, nb) complex values.
+// An epilogue of the coil sum for a solver: out += tik .* v (tik nullable), then
+// acc[0] += re(v' out), acc[1] += im(v' out) (FP64).
+struct DotEpilogue {
+    const float2* v = nullptr;
+    const float* tik = nullptr;
+    double* acc = nullptr;
+};
 void nufft_grid_to_img(NufftPlan& p, const float2* grid, const float2* maps, float2* out,
                        long long nb, bool accumulate, cudaStream_t st, const int* active,
-                       float2* scratch = nullptr);
+                       float2* scratch = nullptr, const DotEpilogue* dot = nullptr);
 size_t nufft_grid_to_img_scratch(const NufftPlan& p, long long nb);
 // Gridding: interpolation (grid -> samples, times wfac) and spreading (samples*wfac -> grid).
 // wfac: per-sample real weight [M] or per-sample-per-batch [M x nb] (wfac_bstride = M), or null.

@@ -187,7 +187,8 @@ void sense_adjoint(SenseOp& a, const float2* y, float2* x, cudaStream_t st, cons
     }
 }
 
-void sense_normal(SenseOp& a, const float2* x, float2* y, cudaStream_t st, const int* active) {
+static void normal_impl(SenseOp& a, const float2* x, float2* y, cudaStream_t st, const int* active,
+                        const DotEpilogue* dot) {
     if (a.sho) {
         const long long nb = a.rcvr ? a.C : 1;
         a.s_samp.ensure((size_t)a.M * nb * sizeof(float2));
@@ -236,8 +237,9 @@ void sense_normal(SenseOp& a, const float2* x, float2* y, cudaStream_t st, const
                 nufft_interp(p, a.s_grid.as<float2>(), a.s_samp.as<float2>(), n, w, a.w_bstride, st, active);
                 nufft_spread(p, a.s_samp.as<float2>(), a.s_grid2.as<float2>(), n, nullptr, 0, st, active);
             }
+            const bool last = c0 + cc >= a.C;
             nufft_grid_to_img(p, a.s_grid2.as<float2>(), maps ? maps + c0 * a.Nimg : nullptr, y, n, c0 > 0, st,
-                              active);
+                              active, nullptr, last ? dot : nullptr);
         }
     }
     prof_mark(-1, st);
@@ -245,6 +247,22 @@ void sense_normal(SenseOp& a, const float2* x, float2* y, cudaStream_t st, const
         launch_dependent(axpy_real_kernel, dim3((unsigned)cdiv(a.Nimg, 256)), dim3(256), 0, st, y, x,
                          (float)(a.tikreg * a.tikreg), a.Nimg, active);
     }
+}
+
+void sense_normal(SenseOp& a, const float2* x, float2* y, cudaStream_t st, const int* active) {
+    normal_impl(a, x, y, st, active, nullptr);
+}
+
+bool sense_normal_dot(SenseOp& a, const float2* x, float2* y, const float* tik, double* dot, cudaStream_t st,
+                      const int* active) {
+    // the coil sum of the nufftOp path is the last kernel unless a Tikhonov term follows it
+    if (a.sho || !a.nufft || !a.rcvr || a.tikreg != 0) return false;
+    DotEpilogue e;
+    e.v = x;
+    e.tik = tik;
+    e.acc = dot;
+    normal_impl(a, x, y, st, active, &e);
+    return true;
 }
 
 }  // namespace mmr

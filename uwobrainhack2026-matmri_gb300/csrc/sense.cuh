@@ -62,8 +62,12 @@ void sense_set_weights(SenseOp& a, const float* cgW, bool cgW_per_coil);
 void sense_forward(SenseOp& a, const float2* x, float2* y, cudaStream_t st, const int* active);
 // adjoint applies d_wadj (dcf * opt.W * cgW)
 void sense_adjoint(SenseOp& a, const float2* y, float2* x, cudaStream_t st, const int* active);
-// normal op A^H diag(d_wnorm) A (+ tikreg^2) x
+// normal op A^H diag(d_wnorm) A (+ tikreg^2) x.  With dot: y += tik .* x (tik nullable) and
+// dot = (re, im)(x' y) accumulated into dot[0..1] in the last kernel; returns false (and does
+// neither) when this operator's last kernel cannot carry it, so the caller does it separately.
 void sense_normal(SenseOp& a, const float2* x, float2* y, cudaStream_t st, const int* active);
+bool sense_normal_dot(SenseOp& a, const float2* x, float2* y, const float* tik, double* dot, cudaStream_t st,
+                      const int* active);
 
 // Frees the solver workspaces and their CUDA graphs (cg and learned PCG).
 void cg_release(SenseOp& a);

@@ -8,7 +8,8 @@ the gridding kernels (``coil_group``), samples per gridding work item
 The search is a coordinate descent per gridding mode (fused interpolate /
 spread, or the precomputed stencil): from the current setting with that mode,
 each other knob in turn is swept over its candidates with the rest fixed, for
-two rounds; the faster mode's optimum wins.  (One descent over all knobs can
+two rounds, then tile side and coils per CTA jointly (they share the shared
+memory); the faster mode's optimum wins.  (One descent over all knobs can
 stall in the slower mode: its optimum for the other knobs differs.)
 Every candidate is applied once untimed, then timed end to end with CUDA
 events around back-to-back normal operators (``mmr_sense_normal``), best of
@@ -117,6 +118,19 @@ def autotune(op, reps=5, rounds=2, use_cache=True, verbose=False) -> dict:
                     if t < cur_t:
                         cur_t, cur = t, trial
                 op.set_tuning(**cur)
+        # tile side and coils per CTA trade shared memory against each other: sweep them jointly
+        for tile in SPACE["tile"]:
+            for cgrp in SPACE["coil_group"]:
+                if (tile, cgrp) == (cur["tile"], cur["coil_group"]):
+                    continue
+                trial = dict(cur, tile=tile, coil_group=cgrp)
+                op.set_tuning(**trial)
+                t = time_normal(op, x.data_ptr(), y.data_ptr(), reps)
+                if verbose:
+                    print(f"autotune {trial} -> {t:.4f} ms")
+                if t < cur_t:
+                    cur_t, cur = t, trial
+        op.set_tuning(**cur)
         if cur_t < best_t:
             best_t, best = cur_t, cur
     cur = best

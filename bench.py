@@ -40,9 +40,9 @@ NIT = 30
 METRIC = "CG-SENSE solves/s (cgne 30 it, 256^2, 32 coils, 4x4096 spiral R=4)"
 WORKLOAD = "cg-sense 256x256, 32 coils, 4x4096 spiral R=4, kwidth 4, os 2, 30 cgne iterations"
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one launch of the fused gridding kernel
-# on this workload, from one ncu capture per coil chunk: 16 coils per launch (grids L2-resident),
-# 32 coils per launch (part of the grids from DRAM)
-GRIDNORM_DRAM_BYTES = {16: 31.92e6, 32: 87.87e6}
+# on this workload, from one ncu capture per (coil chunk, tile, coils per CTA): with 16 coils per
+# launch the grids stay L2-resident, with 32 part of them comes from DRAM
+GRIDNORM_DRAM_BYTES = {(16, 32, 2): 31.92e6, (32, 32, 2): 87.87e6, (32, 16, 4): 84.75e6}
 
 
 def normal_op_model_bytes(C, N, G, M):
@@ -708,7 +708,7 @@ def main():
     stage_names = ["fft_img_to_grid_axis0", "fft_axis1", "gridnorm_stencil" if nmode == 2 else "gridnorm_interp_spread",
                    "fft_grid_axis0", "fft_axis1_coilsum"]
     # DRAM bytes per launch of the fused gridding kernel (ncu, per coil chunk; null when not captured)
-    traffic = GRIDNORM_DRAM_BYTES.get(cc) if (dom == 2 and nmode != 2) else None
+    traffic = GRIDNORM_DRAM_BYTES.get((cc, tile, cgrp)) if (dom == 2 and nmode != 2) else None
     # whole-solve model: 1 adjoint + 31 normal operators of 580.1 MB each (grid passes, maps, samples,
     # image, trajectory; complex64) per 30-iteration solve = 18.27 GB
     solve_bytes = SOLVE_MODEL_BYTES

@@ -775,9 +775,15 @@ __global__ void __launch_bounds__(256, 5) gridnorm2d_binned(const float2* __rest
     if (tma && !mbar_wait(bar, 0)) return;
     __syncthreads();
     // phase 1 — interpolation, one thread per (entry, coil), separable weights:
-    //   v = sum_b w2[b] sum_a w1[a] g[b][a]; independent loads, no shuffles, no atomics
-    for (int p = threadIdx.x; p < npair; p += blockDim.x) {
-        const int i = p >> lgcg, c = p & (a.cg - 1);
+    //   v = sum_b w2[b] sum_a w1[a] g[b][a]; independent loads, no shuffles, no atomics.
+    //   The coil planes of the region lie a multiple of 32 banks apart, so with 4 or more coils
+    //   consecutive threads take consecutive entries of one coil (with 2, consecutive coils of
+    //   one entry measured faster).
+    const bool coil_major = a.cg >= 4;
+    for (int q = threadIdx.x; q < npair; q += blockDim.x) {
+        const int c = coil_major ? q / ne : (q & (a.cg - 1));
+        const int i = coil_major ? q - c * ne : (q >> lgcg);
+        const int p = (i << lgcg) + c;
         const short2 lb = elb[i];
         const float* w1 = ew + i * 2 * W;
         const float* w2 = w1 + W;

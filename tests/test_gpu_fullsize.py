@@ -74,7 +74,8 @@ def test_cgne_matches_fp64(case, nit, tol):
     # rounding with the iterations at this size and conditioning (about 3.6e-4 after 10), so the
     # iterate's tolerance grows with nit.  The residual vector is complex64: its recursively
     # updated norm carries errors of order 1e-7 |r0|, which matter once |r| falls below 1e-4 |r0|,
-    # so residual norms must agree to 1e-3 relative or to 1e-6 |r0|.
+    # so residual norms must agree to 1e-3 relative or to 1e-6 |r0|; |x|^2 to twice the iterate's
+    # tolerance.
     mm, c, Sr, Rr = case
     from matmri_gb300 import synth
     A = _op(mm, c, TUNINGS[0])
@@ -87,4 +88,4 @@ def test_cgne_matches_fp64(case, nit, tol):
     assert rel(x, xr) < tol
     r, rr = np.sqrt(np.asarray(rs)), np.sqrt(rsr.real)
     assert np.all(np.abs(r - rr) <= 1e-3 * rr + 1e-6 * rr[0])
-    assert np.allclose(xn, xnr.real, rtol=1e-4)
+    assert np.allclose(xn, xnr.real, rtol=2 * tol)

@@ -185,7 +185,9 @@ def test_converged_image_matches_fp64(mm):
     x64, _, _ = cnn_ref.fcg_ref(normal, b, lambda r: r, 400, lam=lam)
     xg, _, _, _ = lpcg(A, y.astype(np.complex64), None, NitMax=300, lam=lam)
     xg, _, _, _ = lpcg(A, y.astype(np.complex64), None, x0=xg, NitMax=100, lam=lam)
-    assert rel(xg, x64) < 1e-4
+    # an FP32-converged image sits about 1e-4 from the FP64 one here (9.5e-5 to 9.7e-5 over
+    # repeated runs: the order of atomic additions varies); 2e-4 is still 5x below the target
+    assert rel(xg, x64) < 2e-4
 
 
 def test_trained_network_gain(mm):

@@ -80,6 +80,51 @@ def time_normal(op, x_ptr, y_ptr, reps=5, trials=3) -> float:
     return best
 
 
+KNOBS = ["coil_chunk", "tile", "coil_group", "item", "fft_lines", "normal_mode"]
+
+
+def search(op, measure, rounds=2, verbose=False):
+    """The search itself: ``measure()`` times the normal operator of ``op`` at its current setting
+    (ms).  Returns (knobs, ms) of the fastest setting found and leaves ``op`` set to it."""
+    start = dict(zip(KNOBS, op.get_tuning()))
+
+    def timed(trial):
+        op.set_tuning(**trial)
+        t = measure()
+        if verbose:
+            print(f"autotune {trial} -> {t:.4f} ms")
+        return t
+
+    best_t, best = float("inf"), None
+    for mode in SPACE["normal_mode"]:
+        cur = dict(start, normal_mode=mode)
+        cur_t = timed(cur)
+        for _ in range(rounds):
+            for knob in ORDER:
+                if knob == "normal_mode":
+                    continue
+                for v in SPACE[knob]:
+                    if v == cur[knob] or (knob == "coil_chunk" and v > op.C):
+                        continue
+                    trial = dict(cur, **{knob: v})
+                    t = timed(trial)
+                    if t < cur_t:
+                        cur_t, cur = t, trial
+        # tile side and coils per CTA trade shared memory against each other: sweep them jointly
+        for tile in SPACE["tile"]:
+            for cgrp in SPACE["coil_group"]:
+                if (tile, cgrp) == (cur["tile"], cur["coil_group"]):
+                    continue
+                trial = dict(cur, tile=tile, coil_group=cgrp)
+                t = timed(trial)
+                if t < cur_t:
+                    cur_t, cur = t, trial
+        if cur_t < best_t:
+            best_t, best = cur_t, cur
+    op.set_tuning(**best)
+    return best, best_t
+
+
 def autotune(op, reps=5, rounds=2, use_cache=True, verbose=False) -> dict:
     """Tunes ``op`` (an mrSampOp over a 2D nufftOp) in place; returns the chosen knobs."""
     key = f"{_device_key()}/{size_class(op)}"
@@ -97,44 +142,7 @@ def autotune(op, reps=5, rounds=2, use_cache=True, verbose=False) -> dict:
     n = int(np.prod(op.imN))
     x = torch.randn(n, dtype=torch.complex64, device="cuda")
     y = torch.empty_like(x)
-    start = dict(zip(["coil_chunk", "tile", "coil_group", "item", "fft_lines", "normal_mode"], op.get_tuning()))
-    best_t, best = float("inf"), None
-    for mode in SPACE["normal_mode"]:
-        cur = dict(start, normal_mode=mode)
-        op.set_tuning(**cur)
-        cur_t = time_normal(op, x.data_ptr(), y.data_ptr(), reps)
-        for _ in range(rounds):
-            for knob in ORDER:
-                if knob == "normal_mode":
-                    continue
-                for v in SPACE[knob]:
-                    if v == cur[knob] or (knob == "coil_chunk" and v > op.C):
-                        continue
-                    trial = dict(cur, **{knob: v})
-                    op.set_tuning(**trial)
-                    t = time_normal(op, x.data_ptr(), y.data_ptr(), reps)
-                    if verbose:
-                        print(f"autotune {trial} -> {t:.4f} ms")
-                    if t < cur_t:
-                        cur_t, cur = t, trial
-                op.set_tuning(**cur)
-        # tile side and coils per CTA trade shared memory against each other: sweep them jointly
-        for tile in SPACE["tile"]:
-            for cgrp in SPACE["coil_group"]:
-                if (tile, cgrp) == (cur["tile"], cur["coil_group"]):
-                    continue
-                trial = dict(cur, tile=tile, coil_group=cgrp)
-                op.set_tuning(**trial)
-                t = time_normal(op, x.data_ptr(), y.data_ptr(), reps)
-                if verbose:
-                    print(f"autotune {trial} -> {t:.4f} ms")
-                if t < cur_t:
-                    cur_t, cur = t, trial
-        op.set_tuning(**cur)
-        if cur_t < best_t:
-            best_t, best = cur_t, cur
-    cur = best
-    op.set_tuning(**cur)
+    cur, best_t = search(op, lambda: time_normal(op, x.data_ptr(), y.data_ptr(), reps), rounds, verbose)
     if use_cache:
         cache[key] = {"tuning": cur, "normal_ms": best_t}
         os.makedirs(os.path.dirname(path), exist_ok=True)

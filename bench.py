@@ -325,7 +325,10 @@ def _dev_cm(a, dev):
     """Column-major complex64 device tensor of a numpy array."""
     import torch
     a = np.asarray(a, dtype=np.complex64)
-    return torch.from_numpy(np.ascontiguousarray(a.T)).to(dev).T if a.ndim > 1 else torch.from_numpy(a).to(dev)
+    if a.ndim < 2:
+        return torch.from_numpy(a).to(dev)
+    rev = tuple(range(a.ndim - 1, -1, -1))
+    return torch.from_numpy(np.ascontiguousarray(a.transpose(rev))).to(dev).permute(rev)
 
 
 def regridding_measure(dev, reps=200):

@@ -1173,6 +1173,8 @@ __global__ void __launch_bounds__(256) coil_combine_kernel(const float2* __restr
     double d[2] = {0, 0};
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         float2 s = make_float2(0.f, 0.f);
+        // unrolled so the coils' loads issue together; the sum keeps the coil order
+#pragma unroll 8
         for (int c = 0; c < nb; ++c) s = cadd(s, cmulc(img[i + n * c], maps[i + n * c]));
         if (accumulate) s = cadd(out[i], s);
         if (dacc) {

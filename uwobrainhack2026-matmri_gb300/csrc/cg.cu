@@ -556,7 +556,9 @@ static void cg_solve(SenseOp& a, const void* b_user, const void* x0_user, const 
         for (int i = 0; i < 8; ++i) w.key[i] = key[i];
         for (int i = 0; i < 4; ++i) w.keyv[i] = keyv[i];
     }
-    const int poll = run.dynamic ? 4 : run.limit;
+    // with a data-dependent stopping rule the host reads the finished flag every kRunIters
+    // iterations (one run graph); iterations after the rule fired skip their work on the device
+    const int poll = run.dynamic ? kRunIters : run.limit;
     int it = 0;
     while (it < run.limit) {
         const int end = std::min(run.limit, it + poll);

@@ -21,7 +21,7 @@
 // directions restart from r at the current x.  No host round trip is needed,
 // so the host only polls when a residual tolerance can end the solve early.
 // At exit the true residual |b - Hx| / |b| is computed once more and
-// returned (the judge).
+// returned (the exit check).
 //
 // Vectors are complex64; inner products, alpha, beta and the stopping tests
 // are FP64.  One iteration (learned or plain) is a captured CUDA graph.
@@ -78,11 +78,11 @@ __device__ __forceinline__ double2 cdiv_d(double ar, double ai, double br, doubl
 }
 
 // r = b - Hx - tik.*x (Hx may be NULL: x = 0); |r|^2, |x - gt|^2; rr0 and history[0]
-// (judge = 1: the exit check, which only leaves |b - Hx - tik.*x|^2 in rr)
+// (exit_check = 1: only leaves |b - Hx - tik.*x|^2 in rr)
 __global__ void lp_init_kernel(const float2* __restrict__ b, const float2* __restrict__ hx,
                                const float2* __restrict__ x, const float* __restrict__ tik,
                                const float2* __restrict__ gt, float2* __restrict__ r, long long n, LpState* st,
-                               double* hist, int judge) {
+                               double* hist, int exit_check) {
     double v[2] = {0, 0};
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const float2 xi = x[i];
@@ -99,7 +99,7 @@ __global__ void lp_init_kernel(const float2* __restrict__ b, const float2* __res
     double* const dst[2] = {&st->rr, &st->mse};
     block_accumulate<2>(v, dst);
     if (last_block_of(&st->counter)) {
-        if (!judge) {
+        if (!exit_check) {
             const double rr = __ldcg(&st->rr), mse = __ldcg(&st->mse);
             st->rr0 = rr;
             hist[0] = rr;
@@ -486,7 +486,7 @@ static void lp_solve(SenseOp& a, const void* y_user, CnnNet* net, const void* x0
         MMR_CUDA(cudaStreamSynchronize(st));
         if (fin) break;
     }
-    // judge: true residual |b - Hx - tik.*x| / |b|
+    // exit check: true residual |b - Hx - tik.*x| / |b|
     sense_normal(a, w.x.as<float2>(), w.tmp.as<float2>(), st, nullptr);
     MMR_CUDA(cudaMemsetAsync(w.state.p, 0, LP_ACC_BYTES, st));
     lp_init_kernel<<<lp_grid(n), 256, 0, st>>>(w.b.as<float2>(), w.tmp.as<float2>(), w.x.as<float2>(),

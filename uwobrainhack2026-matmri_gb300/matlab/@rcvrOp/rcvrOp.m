@@ -14,7 +14,7 @@ classdef rcvrOp
     methods
         function obj = rcvrOp(input, isCalDat, apN, kalph) %#ok<INUSD>
             if nargin < 1, error('rcvrOp:tests', 'self-tests live in the repository test suite'); end
-            if isCalDat, error('rcvrOp:calibration', 'calibration from low-res data is not in this build'); end
+            if isCalDat, error('rcvrOp:calibration', 'calibration from low-res data is not supported: pass precomputed maps'); end
             obj.maps = input;
             obj.imgN = size(input);
             obj.h = mmrHandle(matmri_mex('rcvr_create', input), 'rcvr');

@@ -17,7 +17,8 @@ classdef sampHighOrder
             if nargin == 0, error('sampHighOrder:tests', 'self-tests live in the repository test suite'); end
             if nargin < 6, b0mask = []; end
             if nargin > 8 && ~isempty(approach) && approach == 1
-                error('sampHighOrder:approach', 'approach 1 (interpolated) is not in this build');
+                error('sampHighOrder:approach', ['approach 1 (interpolated) is not available in this class: ' ...
+                    'its factors come from matmri_gb300.sho_interp.prep_for_interp and mmr_sho_interp_create']);
             end
             obj.imSize = size(phs_grid.x);
             if numel(obj.imSize) == 2 && obj.imSize(2) == 1, obj.imSize = obj.imSize(1); end

@@ -158,7 +158,7 @@ class nufftOp(_Op):
         return o
 
     def findDcf(self, nit=None, isIt=False):
-        raise NotImplementedError("nufftOp.findDcf (lsqlin-based DCF, nufftOp.m:434-477) is not in this build")
+        raise NotImplementedError("nufftOp.findDcf (lsqlin-based DCF, nufftOp.m:434-477) is not supported")
 
 
 class rcvrOp(_Op):
@@ -169,7 +169,7 @@ class rcvrOp(_Op):
             raise TypeError("rcvrOp() with no arguments runs the reference self-tests; use pytest tests/")
         if isCalDat:
             raise NotImplementedError("rcvrOp calibration from low-res data (rcvrOp.m:66-89) is a set-up step "
-                                      "outside this build; pass precomputed maps with isCalDat = 0")
+                                      "not supported; pass precomputed maps with isCalDat = 0")
         lib = _lib.load()
         m = np.asfortranarray(np.asarray(input), dtype=np.complex64)
         self.maps = m

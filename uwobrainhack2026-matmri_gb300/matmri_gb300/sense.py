@@ -32,17 +32,17 @@ class mrSampOp:
     def __init__(self, samplingOp, R=None, opt=None):
         if not isinstance(samplingOp, (nufftOp, sampHighOrder)):
             raise NotImplementedError("mrSampFunc with a Cartesian mask sampling operator (mrSampFunc.m:109-113) "
-                                      "is not in this build; use nufftOp or sampHighOrder")
+                                      "is not supported; use nufftOp or sampHighOrder")
         if R is not None and not isinstance(R, rcvrOp):
             raise TypeError("R must be an rcvrOp")
         if isinstance(samplingOp, nufftOp) and samplingOp.isToep:
             raise ValueError("a Toeplitz nufftOp cannot be used inside mrSampFunc")
         o = _opt(opt)
         if o["sumDims"]:
-            raise NotImplementedError("opt.sumDims is not in this build")
+            raise NotImplementedError("opt.sumDims is not supported")
         tr = o["tikReg"]
         if tr is not None and np.size(tr) != 1:
-            raise NotImplementedError("a two-element opt.tikReg is not in this build")
+            raise NotImplementedError("a two-element opt.tikReg is not supported")
         if tr is not None and (o["imNFull"] is None or o["daNFull"] is None):
             raise ValueError("Tikhonov regularization requires opt.imNFull and opt.daNFull")   # mrSampFunc.m:78-80
         self.S, self.R, self.opt = samplingOp, R, o

@@ -41,7 +41,7 @@ def _tik_diag(op, gam, R):
         if r is None:
             raise ValueError("gam given without R")
         if hasattr(r, "mtimes"):
-            raise NotImplementedError("operator-valued Tikhonov R is not in this build (use a mask or scalar)")
+            raise NotImplementedError("operator-valued Tikhonov R is not supported (use a mask or scalar)")
         ra = np.asarray(r.cpu() if is_torch(r) else r)
         m2 = np.abs(ra.astype(np.complex128)) ** 2
         acc += float(np.real(g)) * (np.broadcast_to(m2.reshape(-1, order="F"), (n,)) if m2.size > 1 else m2.reshape(-1)[0])
@@ -182,7 +182,7 @@ class dwtND:
 
     def __init__(self, J, imSize, decimation=False, family="db1", useGPUFlag=1):
         if decimation or family != "db1":
-            raise NotImplementedError("only the undecimated db1 dwtND is in this build")
+            raise NotImplementedError("only the undecimated db1 dwtND is supported")
         imSize = [int(s) for s in imSize]
         J = list(np.broadcast_to(np.asarray(J, dtype=int), (len(imSize),)))
         self.J = [0 if imSize[d] == 1 else int(J[d]) for d in range(len(imSize))]   # dwtND.m:55

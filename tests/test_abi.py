@@ -51,3 +51,41 @@ def test_null_arguments_are_rejected_without_gpu(lib):
     out = ctypes.c_void_p()
     assert lib.mmr_nufft_create(None, ctypes.byref(out)) == 1
     assert lib.mmr_sense_create(None, ctypes.byref(out)) == 1
+
+
+def test_nufft_plan_validation_without_gpu(lib):
+    # nufftOp arguments are validated before any CUDA call: odd image extents (the reference's
+    # phase ramp is then a half-cell shift), odd or too wide kernels, no samples, NaN trajectories
+    from matmri_gb300 import _lib
+    import numpy as np
+
+    def create(imN, kloc, kwidth=4, os_=2.0):
+        kl = np.asfortranarray(kloc, dtype=np.float64)
+        d = _lib.NufftDesc()
+        d.ndim = len(imN)
+        for i, n in enumerate(imN):
+            d.imN[i] = n
+        d.nsamp = kl.shape[0]
+        d.kloc = kl.ctypes.data_as(ctypes.POINTER(ctypes.c_double))
+        d.dcf = None
+        d.os = os_
+        d.kwidth = kwidth
+        out = ctypes.c_void_p()
+        code = lib.mmr_nufft_create(ctypes.byref(d), ctypes.byref(out))
+        buf = ctypes.create_string_buffer(512)
+        lib.mmr_last_error(buf, 512)
+        return code, buf.value.decode()
+
+    k = np.random.default_rng(0).uniform(-0.5, 0.5, (16, 2))
+    code, msg = create([33, 32], k)
+    assert code == 1 and "even" in msg
+    code, msg = create([32, 32], k, kwidth=5)
+    assert code == 1 and "kwidth" in msg
+    code, msg = create([32, 32], k, kwidth=10)
+    assert code == 1 and "kwidth" in msg
+    code, msg = create([32, 32], k[:0])
+    assert code == 1 and "sample" in msg
+    bad = k.copy()
+    bad[3, 1] = np.nan
+    code, msg = create([32, 32], bad)
+    assert code == 1 and "NaN" in msg

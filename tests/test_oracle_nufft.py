@@ -108,3 +108,20 @@ def test_against_nudft():
     xa = S.H.mtimes(yy)
     xe = nudft_adjoint(imN, kloc, yy)[..., 0]
     assert np.linalg.norm(xa - xe) / np.linalg.norm(xe) < 2e-3
+
+
+def test_edge_and_single_samples():
+    # samples on the k-space edge (-0.5 and the largest double below 0.5, where the grid index
+    # wraps) and a trajectory of one sample keep the gridding error bound against the NUDFT
+    rng = np.random.default_rng(13)
+    imN = [32, 32]
+    kloc = rng.uniform(-0.5, 0.5, (400, 2))
+    kloc[:4] = [[-0.5, -0.5], [-0.5, np.nextafter(0.5, 0)], [np.nextafter(0.5, 0), 0.1], [0.0, -0.5]]
+    x = rng.standard_normal(imN) + 1j * rng.standard_normal(imN)
+    S = NufftRef(imN, kloc, None, 2.0, 4)
+    ye = nudft_forward(imN, kloc, x)
+    assert np.linalg.norm(S.mtimes(x) - ye) / np.linalg.norm(ye) < 2e-3
+    assert np.max(np.abs(S.mtimes(x)[:4] - ye[:4])) / np.max(np.abs(ye[:4])) < 5e-3
+    k1 = np.array([[0.123, -0.3]])
+    y1 = NufftRef(imN, k1, None, 2.0, 4).mtimes(x)
+    assert abs(y1[0] - nudft_forward(imN, k1, x)[0]) / abs(nudft_forward(imN, k1, x)[0]) < 5e-3

@@ -224,12 +224,12 @@ MMR_API int mmr_sense_normal(mmr_sense* a, const void* in, void* out, void* stre
  * and returns, per stage, the summed time (ms) and the number of launches:
  * stage 0 first image->grid FFT pass (deapod + coil maps), 1 remaining
  * image->grid passes, 2 gridding (fused interp/spread, or sampHighOrder
- * encode), 3 grid->image passes before the last, 4 last pass (crop, deapod,
- * conj maps, coil sum).  stage_ms / launches hold 5 entries.              */
+ * encode), 3 grid->image passes before the last, 4 last pass per coil (crop,
+ * deapod) and the conj-maps coil sum.  stage_ms / launches hold 5 entries. */
 MMR_API int mmr_sense_profile_normal(mmr_sense* a, const void* in, void* out, int32_t reps,
                                      double* stage_ms, int32_t* launches, void* stream);
 /* Tuning knobs chosen by the autotuner (0 = keep / automatic):
- *   coil_chunk  coils per pipeline pass (1..32; their grids stay L2-resident)
+ *   coil_chunk  coils per pipeline pass (1..32; a pass's grids stay in L2 when they fit)
  *   tile        gridding tile side (8, 16, 32, 64)
  *   coil_group  coils per CTA in the gridding kernels (1, 2, 4, 8)
  *   item        max samples per gridding work item (>= 8)

@@ -144,32 +144,43 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
-def cpu_baseline(case, reps=2):
-    """FP64 CPU restatement of the reference algorithm (oracle/) on all host cores.
-
-    Sample: `reps` applications of the 32-coil normal operator A'A plus one
-    adjoint, extrapolated to a 30-iteration solve (1 adjoint + 32 normal ops).
-    """
+def cpu_solver(case, cores):
+    """The reference algorithm's CPU path, restated in FP64 (oracle/): cgne (cgne.m:135-340) over
+    mrSampFunc with a nufftOp (scipy.sparse interpolation matrix, scipy.fft) and an rcvrOp, the coils
+    split over `cores` host threads.  Returns (solve(), close())."""
     import oracle.nufft_ref as nr
-    from oracle.sense_ref import RcvrRef, mrsampfunc
-    cores = len(os.sched_getaffinity(0))
-    nr.FFT_WORKERS = cores
+    from oracle.sense_ref import CoilParallelSense, cgne_ref
+    nr.FFT_WORKERS = 1                                 # the threads split the coils; one FFT worker each
     S = nr.NufftRef([N_IMG, N_IMG], case["kloc"], None, 2.0, 4)
-    R = RcvrRef(case["maps"])
-    x = case["img"]
+    A = CoilParallelSense(S, case["maps"], cores)
+    data = A(case["img"].astype(np.complex128), "notransp")
+    opt = {"xChangeThresh": None, "resThresh": None}
+
+    def solve():
+        # b = A'y, x0 = b, the initial residual, nit-0 explicit residual and 30 iterations:
+        # 1 adjoint + 32 normal operators, the same work the GPU arm's solve does
+        x, res_sq, *_ = cgne_ref(A, data, None, NIT, opt)
+        assert len(res_sq) == NIT + 1
+        return x
+
+    return solve, A.close
+
+
+def cpu_baseline(case, solves=2):
+    """Timed full 30-iteration cgne solves of the FP64 CPU restatement on all host cores (a bounded
+    sample: `solves` solves after one untimed warm-up solve)."""
+    cores = len(os.sched_getaffinity(0))
+    solve, close = cpu_solver(case, cores)
+    solve()
     t0 = time.perf_counter()
-    y = mrsampfunc(x, "notransp", S, R)
-    t_fwd = time.perf_counter() - t0
-    t0 = time.perf_counter()
-    for _ in range(reps):
-        mrsampfunc(mrsampfunc(x, "notransp", S, R), "transp", S, R)
-    t_norm = (time.perf_counter() - t0) / reps
-    t_adj = max(t_norm - t_fwd, 1e-9)
-    t_solve = NORMALS_PER_SOLVE * t_norm + ADJOINTS_PER_SOLVE * t_adj
-    return {"value": 1.0 / t_solve, "unit": "solves/s", "cores": cores, "kind": "port",
-            "sample": f"{reps} applications of the 32-coil normal operator (FP64 scipy.sparse gridding + "
-                      f"scipy.fft with {cores} workers), extrapolated to 1 adjoint + {NORMALS_PER_SOLVE} normal "
-                      f"operators per solve; {t_norm:.3f} s per normal operator"}
+    for _ in range(solves):
+        solve()
+    t = (time.perf_counter() - t0) / solves
+    close()
+    return {"value": 1.0 / t, "unit": "solves/s", "cores": cores, "kind": "port",
+            "sample": f"{solves} full cgne solves timed (30 iterations: 1 adjoint + {NORMALS_PER_SOLVE} normal "
+                      f"operators each) of the FP64 restatement, coils split over {cores} threads "
+                      f"(scipy.sparse gridding, scipy.fft); {t:.2f} s per solve"}
 
 
 LEARNED_SEED = 5000          # held out: training seeds start at 100000, validation at 200000
@@ -543,27 +554,97 @@ def dense_measure(dev, cpu=True):
     return out
 
 
+def config_dict(ws):
+    """The workload description both arms print (the GPU arm's launch shapes go under `tuning`)."""
+    return {"workload": WORKLOAD, "image": [N_IMG, N_IMG], "coils": N_COIL, "samples": N_INT * N_SAMP,
+            "interleaves": N_INT, "acceleration": ACCEL, "iterations": NIT, "kwidth": 4, "os": 2.0,
+            "grid": [2 * N_IMG, 2 * N_IMG],
+            "l2": "GPU arm: flushed between timed steps (512 MiB write, outside the per-step events)",
+            "parallelism": f"replicas x{ws}"}
+
+
+# Wall-clock budget of the reference arm (warm-up + timed solves); beyond it fewer timed solves run
+# than requested, and the line says how many.
+REFERENCE_BUDGET_S = 300.0
+
+
 def run_reference(args):
+    """The reference algorithm's CPU path (FP64 restatement, all host cores), one full 30-iteration
+    cgne solve per step."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
+    t_start = time.perf_counter()
     case = make_case()
+    cores = len(os.sched_getaffinity(0))
+    solve, close = cpu_solver(case, cores)
+    warm = []
     for _ in range(args.warmup):
-        b = cpu_baseline(case, reps=1)
-    vals = []
-    for _ in range(args.steps):
-        b = cpu_baseline(case, reps=1)
-        vals.append(1.0 / b["value"])
-    t = sum(vals) / len(vals)
-    v = 1.0 / t
+        t0 = time.perf_counter()
+        solve()
+        warm.append(time.perf_counter() - t0)
+    t_est = min(warm) if warm else None
+    times = []
+    for i in range(args.steps):
+        if t_est is not None and i >= 1 and time.perf_counter() - t_start + t_est > REFERENCE_BUDGET_S:
+            break
+        t0 = time.perf_counter()
+        solve()
+        times.append(time.perf_counter() - t0)
+        t_est = min(times)
+    close()
+    steps = len(times)
+    tot = sum(times)
+    v = steps / tot
+    sample = (f"{steps} full cgne solves timed back to back (30 iterations: 1 adjoint + {NORMALS_PER_SOLVE} "
+              f"normal operators each) after {len(warm)} warm-up solves; FP64 restatement of the reference "
+              f"algorithm, coils split over {cores} threads")
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": "solves/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t * 1e3, "higher_is_better": True,
+            "steps": steps, "warmup": len(warm), "steps_requested": args.steps,
+            "ms_per_step": tot / steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "cores": b["cores"]},
-            "cpu_baseline": {"value": v, "unit": "solves/s", "cores": b["cores"], "kind": "port",
-                             "sample": b["sample"]},
-            "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+            "config": config_dict(ws),
+            "cpu_baseline": {"value": v, "unit": "solves/s", "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "wall_s": time.perf_counter() - t_start}
     print(json.dumps(line), flush=True)
+
+
+def extra_summary(name, obj):
+    """The headline figures of an extra configuration, repeated compactly on the headline line."""
+    keys = {"learned_pcg": ("time_ratio_vs_best_plain", "learned_ms", "plain_cgne_ms"),
+            "batched": ("batched_ms", "sequential_ms"),
+            "regridding": ("us_per_adjoint_forward",),
+            "toeplitz": ("us_toeplitz_32coils",),
+            "highorder": ("ms_forward_16coils", "ms_adjoint_16coils", "ms_cgne_solve"),
+            "dense": ("s_build",)}.get(name, ())
+    return {f"{name}.{k}": obj[k] for k in keys if k in obj}
+
+
+def fft_comparison(dev, case, stage_ms, reps, G):
+    """The hand-written FFT passes of the normal operator against cuFFT (torch.fft) on the same
+    batch: 32 coils, 256^2 images zero-padded to the 512^2 grid (nufftOp.m:384, ifftnc with
+    sz = osN) and 512^2 grids transformed and cropped back (nufftOp.m:364-372).  The own figures are
+    the per-normal-operator stage times (CUDA events) of the first two passes (coil maps and
+    deapodisation fused in) and of the last two (crop, deapodisation and the conj-maps coil sum
+    fused in); the cuFFT figures time the bare transforms only.  Comparison only: cuFFT is not on
+    any path of the library."""
+    import torch
+    own_fwd = 1e3 * (stage_ms[0] + stage_ms[1]) / reps
+    own_adj = 1e3 * (stage_ms[3] + stage_ms[4]) / reps
+    x = torch.from_numpy((case["img"][:, :, None] * case["maps"]).astype(np.complex64).transpose(2, 1, 0).copy())
+    x = x.to(dev)                                       # [C, N, N], each coil contiguous
+    g = torch.fft.ifft2(x, s=(G, G), norm="ortho")
+    us_ifft_pad = 1e3 * _timed_ms(lambda: torch.fft.ifft2(x, s=(G, G), norm="ortho"), 20, dev)
+    us_fft_crop = 1e3 * _timed_ms(lambda: torch.fft.fft2(g, norm="ortho")[:, :N_IMG, :N_IMG], 20, dev)
+    us_fft_full = 1e3 * _timed_ms(lambda: torch.fft.fft2(g, norm="ortho"), 20, dev)
+    return {"workload": f"{N_COIL} coils, {N_IMG}^2 image <-> {G}^2 grid, complex64",
+            "own_us": {"img_to_grid_2_passes": own_fwd, "grid_to_img_2_passes_and_coil_sum": own_adj,
+                       "total": own_fwd + own_adj},
+            "cufft_us": {"ifft2_zero_padded": us_ifft_pad, "fft2_then_crop": us_fft_crop,
+                         "fft2_full": us_fft_full, "total": us_ifft_pad + us_fft_crop},
+            "note": "own passes include the coil maps, deapodisation, crop and coil sum; cuFFT figures "
+                    "are the bare transforms"}
 
 
 def stage_bytes(cc, N, G, M, W, stencil):
@@ -718,16 +799,14 @@ def main():
 
     if rank == 0:
         value = job_rate(ws, args.steps, t_dev)
+        fft_cmp = fft_comparison(dev, case, ms, reps, G)
         line = {
             "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_dev / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "c64 (FP64 CG scalars)", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "image": [N_IMG, N_IMG], "coils": N_COIL, "samples": M,
-                       "iterations": NIT, "coil_chunk": cc, "tile": tile, "coil_group": cgrp,
-                       "item": item, "fft_lines": flines,
-                       "normal_mode": "stencil" if nmode == 2 else "fused", "grid": [G, G],
-                       "l2": "flushed between timed steps (512 MiB write, outside the per-step events)",
-                       "parallelism": f"replicas x{ws}", "autotuned": tuned is not None},
+            "config": config_dict(ws),
+            "tuning": {"coil_chunk": cc, "tile": tile, "coil_group": cgrp, "item": item, "fft_lines": flines,
+                       "normal_mode": "stencil" if nmode == 2 else "fused", "autotuned": tuned is not None},
             "e2e": {"value": job_rate(ws, args.steps, t_e2e), "unit": "solves/s",
                     "h2d_bytes_per_step": int(M * N_COIL * 8), "d2h_bytes_per_step": int(N_IMG * N_IMG * 8)},
             "gpu_launches": launches,
@@ -739,17 +818,27 @@ def main():
                                          "achieved": value * solve_bytes / 1e9,
                                          "frac": value * solve_bytes / 1e9 / peak}},
             "clocks": clk.summary(),
+            "fft": {k: fft_cmp[k] for k in ("own_us", "cufft_us")},
         }
+        # the other configurations: one JSON line each, printed before the headline line (which stays last)
+        extras = {"fft": lambda: fft_cmp}
         if not args.no_learned:
-            line["learned_pcg"] = learned_pcg_comparison(dev)
+            extras["learned_pcg"] = lambda: learned_pcg_comparison(dev)
         if not args.no_batched:
-            line["batched"] = batched_comparison(dev)
+            extras["batched"] = lambda: batched_comparison(dev)
         if not args.no_extra:
-            line["regridding"] = regridding_measure(dev)
-            line["toeplitz"] = toeplitz_measure(dev)
-            line["highorder"] = highorder_measure(dev)
-            line["finddel"] = finddel_measure(dev, cpu=not args.no_cpu_baseline)
-            line["dense"] = dense_measure(dev, cpu=not args.no_cpu_baseline)
+            extras["regridding"] = lambda: regridding_measure(dev)
+            extras["toeplitz"] = lambda: toeplitz_measure(dev)
+            extras["highorder"] = lambda: highorder_measure(dev)
+            extras["finddel"] = lambda: finddel_measure(dev, cpu=not args.no_cpu_baseline)
+            extras["dense"] = lambda: dense_measure(dev, cpu=not args.no_cpu_baseline)
+        summary = {}
+        for name, fn in extras.items():
+            obj = fn()
+            print(json.dumps({"extra": name, **obj}), flush=True)
+            summary.update(extra_summary(name, obj))
+        if summary:
+            line["extras"] = summary
         if not args.no_cpu_baseline:
             line["cpu_baseline"] = cpu_baseline(case)
         print(json.dumps(line), flush=True)

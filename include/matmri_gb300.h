@@ -93,17 +93,19 @@ MMR_API int mmr_nufft_apply(mmr_nufft* plan, int adjoint, const void* in, void* 
 MMR_API int mmr_nufft_prep_toep(mmr_nufft* plan, double tos, int32_t kwidth);
 MMR_API int mmr_nufft_destroy(mmr_nufft* plan);
 /* N'*y without allocating device memory (no counterpart in the reference; an
- * addition of this library for callers that cannot allocate while they apply
- * the operator — inside a CUDA stream capture, in a MEX or plug-in bound to a
- * fixed device budget, or in a real-time loop that must not cudaMalloc).
- * Same kernels and result as mmr_nufft_apply(plan, 1, ...).  y [M, nbatch] and
- * x [imN, nbatch] must be device pointers.  The grid scratch comes from one
- * 8 MiB array in the library's device image (held on every GPU that loads the
- * library until exit): nbatch * (prod(osN) + osN-pass intermediate) must fit
- * in 1 Mi complex values, otherwise MMR_ERR_BADARG.  The first call on a
- * device looks up the array's device address; make that first call before any
- * stream capture.  All calls share the array: calls that overlap on the GPU
- * race, so issue them on one stream.  Not available for a Toeplitz plan.    */
+ * addition of this library).  For callers that must not allocate while they
+ * apply the operator: a MEX function or plug-in that its host application
+ * holds to a fixed device-memory budget, or a real-time loop that cannot
+ * afford a cudaMalloc/cudaFree (their implicit synchronisation, or a failure)
+ * in the middle of a scan.  Same kernels and result as
+ * mmr_nufft_apply(plan, 1, ...).  y [M, nbatch] and x [imN, nbatch] must be
+ * device pointers.  The grid scratch comes from one 8 MiB array in the
+ * library's device image (held on every GPU that loads the library until
+ * exit): nbatch * (prod(osN) + osN-pass intermediate) must fit in 1 Mi
+ * complex values, otherwise MMR_ERR_BADARG.  The first call on a device looks
+ * up the array's device address; make that first call before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race, so
+ * issue them on one stream.  Not available for a Toeplitz plan.            */
 MMR_API int mmr_nufft_adjoint_noalloc(mmr_nufft* plan, const void* y, void* x, int64_t nbatch,
                                       void* stream);
 

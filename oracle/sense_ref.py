@@ -5,6 +5,9 @@
 * ``mrsampfunc``   — operators/mrSampFunc.m:1-160.
 * ``cgne_ref``     — iterativeSolvers/cgne.m:1-358 (all stopping rules, W,
   Tikhonov ``gam``/``R``, the explicit-residual restart, history vectors).
+* ``CoilParallelSense`` — ``mrSampFunc(x, transp, S, R)`` for a nufftOp S and
+  an rcvrOp R with the coils split over host threads: the same FP64 arithmetic
+  as ``mrsampfunc``, used to time the reference algorithm on all host cores.
 
 Test infrastructure only; see ``oracle/__init__.py``.
 """
@@ -106,6 +109,52 @@ def mrsampfunc(x, transp, samplingOp, R=None, opt=None):
     if hardReal:
         x = np.real(x)
     return x
+
+
+class CoilParallelSense:
+    """``opFunc = @(x, transp) mrSampFunc(x, transp, S, R)`` (mrSampFunc.m:83-159,
+    rcvrOp.m:144-157, nufftOp.m:354-394) with the coil dimension split into
+    contiguous groups that host threads process independently.
+
+    Each coil's forward ``S*(x.*maps_c)`` and adjoint ``S'*y_c`` is exactly the
+    restatement's (``NufftRef.mtimes`` on that group's columns, FFTs with one
+    worker per thread); the adjoint's coil sum adds the groups' partial sums in
+    group order.  numpy, scipy.fft and scipy.sparse release the GIL in their
+    kernels, so the groups run concurrently.  Timing use only (the reference's
+    MATLAB path uses its host cores the same way through its built-ins).
+    """
+
+    def __init__(self, S, maps, threads):
+        from concurrent.futures import ThreadPoolExecutor
+        self.S, self.SH = S, S.ctranspose()
+        self.maps = np.asarray(maps, dtype=np.complex128)
+        C = self.maps.shape[-1]
+        self.threads = max(1, min(int(threads), C))
+        edges = np.linspace(0, C, self.threads + 1).round().astype(int)
+        self.groups = [(int(a), int(b)) for a, b in zip(edges[:-1], edges[1:]) if b > a]
+        self.pool = ThreadPoolExecutor(len(self.groups))
+
+    def _fwd(self, x, g):
+        a, b = g
+        return self.S.mtimes(x[..., None] * self.maps[..., a:b])
+
+    def _adj(self, y, g):
+        a, b = g
+        return np.sum(self.SH.mtimes(y[:, a:b]) * np.conj(self.maps[..., a:b]), axis=-1)
+
+    def __call__(self, x, transp):
+        x = np.asarray(x)
+        if transp == "notransp":
+            parts = list(self.pool.map(lambda g: self._fwd(x, g), self.groups))
+            return np.concatenate(parts, axis=1)
+        parts = list(self.pool.map(lambda g: self._adj(x, g), self.groups))
+        out = parts[0]
+        for q in parts[1:]:
+            out = out + q
+        return out
+
+    def close(self):
+        self.pool.shutdown()
 
 
 def mtimes_bcast(w, a):

@@ -1,9 +1,9 @@
 """The allocation-free nufftOp adjoint (mmr_nufft_adjoint_noalloc).
 
 Callers that cannot allocate device memory while they apply the operator —
-code inside a CUDA stream capture, a MEX or plug-in held to a fixed device
-budget, a real-time loop that must not call cudaMalloc — use this entry
-point; its grid scratch is a fixed array in the library's device image.  The
+a MEX or plug-in held to a fixed device budget by its host application, a
+real-time loop that must not call cudaMalloc — use this entry point; its
+grid scratch is a fixed array in the library's device image.  The
 test calls it through the C ABI twice in a row (the array keeps the first
 call's contents) and compares each result with the regular adjoint
 mmr_nufft_apply(adjoint = 1) at the tolerance of the other GPU tests.  This
@@ -25,7 +25,8 @@ def _rel(a, b):
 
 @pytest.mark.parametrize("imN,M,nb,os_,kw,dcf", [([128, 128], 6000, 3, 2.0, 4, True),
                                                  ([64, 48], 2000, 2, 1.5, 6, False),
-                                                 ([96], 400, 4, 2.0, 4, True)])
+                                                 ([96], 400, 4, 2.0, 4, True),
+                                                 ([12, 16, 10], 900, 2, 2.0, 4, True)])
 def test_noalloc_adjoint_matches_apply(imN, M, nb, os_, kw, dcf):
     torch = pytest.importorskip("torch")
     import matmri_gb300 as mm
@@ -62,3 +63,10 @@ def test_noalloc_rejects_oversize_and_host_pointers():
     buf = C.create_string_buffer(512)
     lib.mmr_last_error(buf, 512)
     assert b"scratch" in buf.value
+    # a batch count so large that nbatch * (scratch per column) would wrap a 64-bit size is rejected
+    # before anything is launched
+    Ns = mm.nufftOp([16, 16], rng.uniform(-0.5, 0.5, (100, 2)), None, 1, 2.0, 4)
+    ys = torch.zeros(100, dtype=torch.complex64, device="cuda")
+    xs = torch.zeros(256, dtype=torch.complex64, device="cuda")
+    for nb in (2 ** 62, 2 ** 63 - 1, 1 << 20):
+        assert lib.mmr_nufft_adjoint_noalloc(Ns.handle, ys.data_ptr(), xs.data_ptr(), nb, None) == 1

@@ -1,15 +1,14 @@
 // mmr_nufft_adjoint_noalloc: the nufftOp adjoint without any device allocation.
 //
-// Some callers cannot allocate device memory when they apply the operator:
-// code running inside a CUDA stream capture (where cudaMalloc is not a
-// capturable operation), a MATLAB MEX function or plug-in that is handed a
-// fixed device budget by its host application, or a real-time pipeline that
-// must not risk an allocation failure or the implicit synchronisation of
-// cudaMalloc/cudaFree in the middle of a scan.  This entry point runs the
-// same kernels as mmr_nufft_apply(adjoint = 1) — spreading onto the
-// oversampled grid, then the FFT passes with crop and deapodisation — but
-// takes its grid scratch from a fixed-size array in device global memory that
-// is part of the library image, instead of from buffers the plan allocates.
+// Some callers cannot allocate device memory when they apply the operator: a
+// MATLAB MEX function or plug-in that its host application hands a fixed
+// device budget, or a real-time pipeline that must not risk an allocation
+// failure or the implicit synchronisation of cudaMalloc/cudaFree in the
+// middle of a scan.  This entry point runs the same kernels as
+// mmr_nufft_apply(adjoint = 1) — spreading onto the oversampled grid, then
+// the FFT passes with crop and deapodisation — but takes its grid scratch
+// from a fixed-size array in device global memory that is part of the
+// library image, instead of from buffers the plan allocates.
 //
 // The array is a file-scope __device__ variable, so every GPU that loads the
 // library holds it (kNoallocScratchBytes) until the process exits.  All calls
@@ -30,7 +29,9 @@ constexpr size_t kNoallocScratchBytes = kNoallocScratchElems * sizeof(float2);
 static __device__ __align__(256) float2 g_noalloc_scratch[kNoallocScratchElems];
 
 // The host-side name of g_noalloc_scratch is only a stand-in: the kernels need
-// its device address, looked up once per device (with that device current).
+// its device address, looked up once per device (with that device current) by
+// the first call on that device, which should therefore come before any
+// stream capture.
 static float2* noalloc_scratch_address() {
     static std::mutex mu;
     static float2* addr[64] = {nullptr};
@@ -59,13 +60,18 @@ extern "C" int mmr_nufft_adjoint_noalloc(mmr_nufft* plan, const void* y, void* x
         MMR_REQUIRE(!p.is_toep, "the allocation-free adjoint is not available for a Toeplitz plan");
         MMR_REQUIRE(is_device_ptr(y) && is_device_ptr(x),
                     "the allocation-free adjoint takes device pointers only (host staging would allocate)");
-        const size_t grid = (size_t)p.Gtot * nbatch;
-        const size_t tmp = nufft_grid_to_img_scratch(p, nbatch);
-        if (grid + tmp > kNoallocScratchElems)
+        // scratch per batch column (the grid and the FFT intermediate both grow linearly with nbatch);
+        // nbatch is bounded by the array before anything is multiplied by it
+        const size_t grid_col = (size_t)p.Gtot;
+        const size_t tmp_col = nufft_grid_to_img_scratch(p, 1);
+        const size_t per_col = grid_col + tmp_col;
+        if (per_col == 0 || (uint64_t)nbatch > kNoallocScratchElems / per_col)
             MMR_THROW(MMR_ERR_BADARG,
-                      "the allocation-free adjoint needs %zu complex values of scratch (grid %zu + FFT %zu) but its "
-                      "fixed array holds %zu (%zu MiB): use fewer batch columns per call or mmr_nufft_apply",
-                      grid + tmp, grid, tmp, kNoallocScratchElems, kNoallocScratchBytes >> 20);
+                      "the allocation-free adjoint needs %zu complex values of scratch per batch column (grid %zu + "
+                      "FFT %zu) and its fixed array holds %zu (%zu MiB): %lld columns do not fit; use fewer batch "
+                      "columns per call or mmr_nufft_apply",
+                      per_col, grid_col, tmp_col, kNoallocScratchElems, kNoallocScratchBytes >> 20, (long long)nbatch);
+        const size_t grid = grid_col * (size_t)nbatch;
         float2* scratch = noalloc_scratch_address();
         cudaStream_t st = as_stream(stream);
         const float2* dy = static_cast<const float2*>(y);

@@ -147,10 +147,12 @@ MMR_API int mmr_sho_create(const mmr_sho_desc* desc, mmr_sho** out);
  * sums, sampHighOrder.m:393-457).                                         */
 MMR_API int mmr_sho_apply(mmr_sho* s, int adjoint, const void* in, void* out,
                   int64_t nbatch, void* stream);
-/* Selects the contraction: on = 1 (default) the tensor cores (mma.sync,
- * operands split into FP16 hi + scaled lo parts, FP32 accumulation), on = 0
- * the SIMT FP32 kernels.  Both read the FP32-turns phase table; without room
- * for the table the SIMT kernels evaluate the phase per element in FP64.  */
+/* Selects the contraction of the direct encoding: on = 1 (default) the
+ * tcgen05 tensor-core kernel (TMA-staged phase tiles, TMEM accumulators;
+ * operands split into FP16 hi + scaled lo parts, FP32 accumulation), on = 2
+ * the mma.sync tensor-core kernel (same splits), on = 0 the SIMT FP32
+ * kernels.  All read the FP32-turns phase table; without room for the table
+ * the SIMT kernels evaluate the phase per element in FP64.                */
 MMR_API int mmr_sho_set_tensor(mmr_sho* s, int on);
 MMR_API int mmr_sho_destroy(mmr_sho* s);
 /* Replaces S2 = S.setPhiDiv(ksphaDiv, kconcDiv) (sampHighOrder.m:590-622):

@@ -82,8 +82,10 @@ def test_headline_30_iteration_cgne_matches_fp64(mm, sense256):
     and by 30 iterations CG resolves directions so weak that any FP32 rounding moves the iterate
     by percents: the FP64 restatement itself, with only its operator outputs rounded to complex64,
     ends 1.6e-2 from the FP64 iterate.  The GPU iterate must stay within 3x of that intrinsic
-    deviation, measured here on the same data; the residual norms must agree to 1e-3 over the
-    first 10 iterations and within a factor 3 after."""
+    deviation, measured here on the same data.  The residual norms must agree to 1e-3 over the
+    first 10 iterations (later, the recursively updated complex64 residual sits at its rounding
+    floor), and the quantity CG minimises, the data misfit |A x - y| (both evaluated with the FP64
+    operator), must agree to 1e-2 at the end (measured 2.3e-3)."""
     from matmri_gb300 import synth
     c, A, Ar = sense256
     data = synth.add_noise(Ar(c["img"].astype(np.complex128), "notransp"), 30.0, 2001)
@@ -98,7 +100,10 @@ def test_headline_30_iteration_cgne_matches_fp64(mm, sense256):
     assert status == statr == 0 and len(rs) == len(rsr) == 31
     assert e < 3 * e32
     assert np.all(np.abs(r[:11] - rr[:11]) <= 1e-3 * rr[:11] + 1e-6 * rr[0])
-    assert np.all(r / rr < 3) and np.all(rr / r < 3)
+    fit = np.linalg.norm(Ar(np.asarray(x, dtype=np.complex128), "notransp") - data)
+    fit_r = np.linalg.norm(Ar(xr, "notransp") - data)
+    print(f"data misfit |Ax - y|: GPU {fit:.6e}, FP64 {fit_r:.6e}")
+    assert abs(fit - fit_r) / fit_r < 1e-2
 
 
 @pytest.mark.parametrize("lam_rel", [1e-3, 1e-2])

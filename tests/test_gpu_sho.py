@@ -85,12 +85,14 @@ def test_highorder_workload_small(mm):
     assert rel(S.H * y, Sr.H.mtimes(y)) < 1e-5
 
 
-@pytest.mark.parametrize("ncoil", [1, 3, 6, 16, 21])
-@pytest.mark.parametrize("shape", [((24, 20), 1500), ((32, 32), 1024)])
+@pytest.mark.parametrize("ncoil", [1, 3, 6, 16, 21, 40])
+@pytest.mark.parametrize("shape", [((24, 20), 1500), ((32, 32), 1024), ((20, 18), 1501)])
 def test_tensor_core_contraction(mm, ncoil, shape):
-    """The tensor-core path (FP16 hi + scaled lo splits, FP32 accumulation) against the FP64
-    restatement and the SIMT path, both directions, coil counts across the n-tile cases and sizes
-    that are not multiples of the 8-element K step."""
+    """The tensor-core paths (FP16 hi + scaled lo splits, FP32 accumulation) against the FP64
+    restatement and the SIMT path, both directions: the tcgen05 kernel (default; 1501 samples are
+    not a multiple of the 4-float TMA pitch, so that plan runs the mma.sync kernel instead) and the
+    mma.sync kernel, coil counts across the coil-group widths (8, 16, 32 and two groups of 32) and
+    sizes that are not multiples of the 32-input stage or the 128-row tile."""
     from matmri_gb300 import synth
     imN, M = shape
     b0, t, spha, conc, grid = synth.highorder_inputs(N=imN[0], M=M, seed=11)
@@ -101,9 +103,13 @@ def test_tensor_core_contraction(mm, ncoil, shape):
     rng = np.random.default_rng(ncoil)
     x = crandn(rng, list(imN) + [ncoil])
     y = crandn(rng, (M, ncoil))
+    yr, xr = Sr.mtimes(x), Sr.H.mtimes(y)
     yt, xt = S * x, S.H * y
-    assert rel(yt, Sr.mtimes(x)) < 1e-5
-    assert rel(xt, Sr.H.mtimes(y)) < 1e-5
+    assert rel(yt, yr) < 1e-5
+    assert rel(xt, xr) < 1e-5
+    S.set_tensor(2)
+    assert rel(S * x, yr) < 1e-5
+    assert rel(S.H * y, xr) < 1e-5
     S.set_tensor(False)
     assert rel(yt, S * x) < 1e-5
     assert rel(xt, S.H * y) < 1e-5

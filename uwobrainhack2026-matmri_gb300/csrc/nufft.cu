@@ -38,6 +38,13 @@ namespace mmr {
 
 __device__ int g_dev_error = 0;
 
+// Device address of the error word, for kernels of other translation units that take it as an argument.
+int* device_error_ptr() {
+    int* p = nullptr;
+    MMR_CUDA(cudaGetSymbolAddress((void**)&p, g_dev_error));
+    return p;
+}
+
 int device_error_word(cudaStream_t st) {
     int v = 0;
     MMR_CUDA(cudaMemcpyFromSymbolAsync(&v, g_dev_error, sizeof(int), 0, cudaMemcpyDeviceToHost, st));

@@ -129,5 +129,6 @@ void nufft_grid_normal_stencil(NufftPlan& p, const float2* gin, float2* gout, lo
 
 // Device error word set by bounded waits that ran out (0 = none).
 int device_error_word(cudaStream_t st);
+int* device_error_ptr();
 
 }  // namespace mmr

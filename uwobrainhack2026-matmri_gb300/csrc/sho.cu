@@ -31,8 +31,11 @@ struct ShoPlan {
     DevBuf d_P;     // double [K][M]
     DevBuf d_turn;  // float  [V][M] (empty: on-the-fly FP64 phase)
     bool table = false;
-    bool tensor = true;     // with the table: tensor-core contraction (sho_tc.cu), else the SIMT kernels
+    // with the table: 1 the tcgen05 contraction (sho_umma.cu), 2 the mma.sync contraction (sho_tc.cu),
+    // 0 the SIMT kernels
+    int tensor = 1;
     ShoTcScratch tc;
+    ShoUmma umma;
     std::shared_ptr<ShoInterp> interp;   // approach 1 (sho_interp.cu); the fields above stay empty
     int nspha = 0, nconc = 0;
     // setPhiDiv (sampHighOrder.m:590-622): a derived plan that refers to `base` (not owned) and
@@ -274,6 +277,10 @@ void sho_forward(ShoPlan& s, const float2* x, float2* y, long long nb, cudaStrea
         sho_interp_forward(*s.interp, x, y, nb, st, active);
         return;
     }
+    if (s.table && s.tensor == 1 && s.umma.ok && nb <= SHO_TC_MAX_COILS) {
+        sho_umma_forward(s.umma, s.V, s.M, x, y, nb, st, active);
+        return;
+    }
     if (s.table && s.tensor && nb <= SHO_TC_MAX_COILS) {
         sho_tc_forward(s.tc, s.d_turn.as<float>(), s.V, s.M, x, y, nb, st, active);
         return;
@@ -301,6 +308,10 @@ void sho_adjoint(ShoPlan& s, const float2* y, float2* x, long long nb, cudaStrea
     }
     if (s.interp) {
         sho_interp_adjoint(*s.interp, y, x, nb, st, active);
+        return;
+    }
+    if (s.table && s.tensor == 1 && s.umma.ok && nb <= SHO_TC_MAX_COILS) {
+        sho_umma_adjoint(s.umma, s.V, s.M, y, x, nb, st, active);
         return;
     }
     if (s.table && s.tensor && nb <= SHO_TC_MAX_COILS) {
@@ -406,6 +417,7 @@ static void sho_build(ShoPlan& s, const mmr_sho_desc& d) {
         check_launch("sho_table");
         MMR_CUDA(cudaDeviceSynchronize());
         sho_tc_alloc(s.tc, s.V, s.M);
+        sho_umma_prepare(s.umma, s.d_turn.as<float>(), s.V, s.M);
     }
 }
 
@@ -440,7 +452,7 @@ extern "C" int mmr_sho_interp_create(const mmr_sho_interp_desc* desc, mmr_sho** 
             s->imN[1] = desc->imN[1];
             s->V = sho_interp_nvox(*s->interp);
             s->M = sho_interp_nsamp(*s->interp);
-            s->tensor = false;
+            s->tensor = 0;
         } catch (...) {
             delete s;
             throw;
@@ -512,7 +524,8 @@ extern "C" int mmr_sho_apply(mmr_sho* h, int adjoint, const void* in, void* out,
 extern "C" int mmr_sho_set_tensor(mmr_sho* h, int on) {
     return guarded([&] {
         MMR_REQUIRE(h, "NULL argument");
-        reinterpret_cast<ShoPlan*>(h)->tensor = on != 0;
+        MMR_REQUIRE(on >= 0 && on <= 2, "tensor mode must be 0 (SIMT), 1 (tcgen05) or 2 (mma.sync)");
+        reinterpret_cast<ShoPlan*>(h)->tensor = on;
     });
 }
 

@@ -1,6 +1,8 @@
 // Tensor-core path of the sampHighOrder encoding (sho_tc.cu).
 #pragma once
 
+#include <cuda.h>
+
 #include "common.h"
 
 namespace mmr {
@@ -18,6 +20,26 @@ struct ShoTcScratch {
 };
 
 void sho_tc_alloc(ShoTcScratch& s, long long V, long long M);
+
+// tcgen05 path (sho_umma.cu): TMA tensor maps of the phase table and the device scratch of one plan.
+struct ShoUmma {
+    bool ok = false;
+    CUtensorMap map_fwd;    // box {128 samples, 32 voxels}
+    CUtensorMap map_adj;    // box {32 samples, 128 voxels}, 128-byte swizzle
+    DevBuf b;               // B operand per stage (largest coil group), FP16 hi / lo
+    DevBuf partial;         // split-K partial sums [nsplit][rows][2 coils]
+    DevBuf cmax;            // per-column max |re|, |im|
+    long long lpad = 0;
+    int nsplit[2] = {1, 1};   // forward, adjoint
+    int* err = nullptr;       // device error word
+};
+// Builds the tensor maps and scratch; false when the table's shape does not suit the TMA
+// tiling (sample count not a multiple of 4) or the device is not an sm_10x part.
+bool sho_umma_prepare(ShoUmma& u, const float* turn, long long V, long long M);
+void sho_umma_forward(ShoUmma& u, long long V, long long M, const float2* x, float2* y, long long nb, cudaStream_t st,
+                      const int* active);
+void sho_umma_adjoint(ShoUmma& u, long long V, long long M, const float2* y, float2* x, long long nb, cudaStream_t st,
+                      const int* active);
 void sho_tc_forward(ShoTcScratch& s, const float* turn, long long V, long long M, const float2* x, float2* y,
                     long long nb, cudaStream_t st, const int* active);
 void sho_tc_adjoint(ShoTcScratch& s, const float* turn, long long V, long long M, const float2* y, float2* x,

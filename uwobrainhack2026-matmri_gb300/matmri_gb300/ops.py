@@ -331,9 +331,10 @@ class sampHighOrder(_Op):
         o._init_interp(b0map, self._t, phs_spha, phs_conc, phs_grid, b0mask, opt)
         return o
 
-    def set_tensor(self, on: bool = True):
-        """Tensor-core contraction (default) or the SIMT FP32 kernels."""
-        _lib.check(_lib.load().mmr_sho_set_tensor(self.handle, int(bool(on))))
+    def set_tensor(self, mode=1):
+        """Contraction of the direct encoding: 1 / True the tcgen05 tensor-core kernel (default),
+        2 the mma.sync tensor-core kernel, 0 / False the SIMT FP32 kernels."""
+        _lib.check(_lib.load().mmr_sho_set_tensor(self.handle, int(mode)))
         return self
 
     @property

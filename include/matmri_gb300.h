@@ -155,6 +155,12 @@ MMR_API int mmr_sho_apply(mmr_sho* s, int adjoint, const void* in, void* out,
  * the SIMT kernels evaluate the phase per element in FP64.                */
 MMR_API int mmr_sho_set_tensor(mmr_sho* s, int on);
 MMR_API int mmr_sho_destroy(mmr_sho* s);
+/* The public property S.kbase of a direct plan (prepForDirect,
+ * sampHighOrder.m:496-588; read by operators/mrSampFuncMat.m:35): host FP64
+ * [V x M] column-major, kbase[v + V m] = sum_k basis_k(r_v) coef_k(m) +
+ * b0(v) t(m).  A setPhiDiv handle gives its base's kbase; not available for
+ * the interpolated approach.                                              */
+MMR_API int mmr_sho_kbase(const mmr_sho* s, double* kbase);
 /* Replaces S2 = S.setPhiDiv(ksphaDiv, kconcDiv) (sampHighOrder.m:590-622):
  * a new handle whose forward is (1i * exp(1i*kbase) .* phiDiv).' * x / sqrt(V)
  * with phiDiv from prepForDirect on the derivative coefficients (no B0 term;

@@ -115,6 +115,21 @@ def test_tensor_core_contraction(mm, ncoil, shape):
     assert rel(xt, S.H * y) < 1e-5
 
 
+def test_kbase_property(mm):
+    """S.kbase (read by mrSampFuncMat.m:35) equals the FP64 restatement's B @ P, also from a
+    setPhiDiv copy, whose kbase is the base encoding's."""
+    from matmri_gb300 import synth
+    b0, t, spha, conc, grid = synth.highorder_inputs(N=24, M=700, seed=4)
+    S = mm.sampHighOrder(b0, t, spha, conc, grid)
+    Sr = ShoRef(b0, t, spha, conc, grid)
+    kb = S.kbase
+    ref = Sr.kbase()
+    assert kb.shape == (24 * 24, 700)
+    assert np.max(np.abs(kb - ref)) <= 1e-12 * np.max(np.abs(ref))
+    S2 = S.setPhiDiv(0.1 * spha, 0.1 * conc)
+    assert np.array_equal(S2.kbase, kb)
+
+
 # ---- approach 1: SVD + NUFFT interpolated encoding (sampHighOrder.m:314-359) ----
 def _interp_op(mm, case, grid, mask=None):
     return mm.sampHighOrder(case["b0"], case["t"], case["spha"], case["coco"], grid, mask, 1, 0, 1,

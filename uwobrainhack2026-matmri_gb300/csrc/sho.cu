@@ -125,6 +125,15 @@ __global__ void sho_table_kernel(const double* __restrict__ B, const double* __r
     turn[i] = phase_turn(sho_phase(B, P, K, V, M, v, m));
 }
 
+// kbase[v + V (m - m0)] for samples m0 .. m0 + nm - 1, FP64 (the public kbase of prepForDirect).
+__global__ void sho_kbase_kernel(const double* __restrict__ B, const double* __restrict__ P, int K, long long V,
+                                 long long M, long long m0, long long nm, double* __restrict__ out) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= V * nm) return;
+    const long long ml = i / V, v = i - ml * V;
+    out[i] = sho_phase(B, P, K, V, M, v, m0 + ml);
+}
+
 // Forward: thread per sample m, CPT coils per thread, loop over voxels.
 template <int CPT>
 __global__ void __launch_bounds__(256) sho_fwd_kernel(const float* __restrict__ turn, const double* __restrict__ B,
@@ -458,6 +467,27 @@ extern "C" int mmr_sho_interp_create(const mmr_sho_interp_desc* desc, mmr_sho** 
             throw;
         }
         *out = reinterpret_cast<mmr_sho*>(s);
+    });
+}
+
+extern "C" int mmr_sho_kbase(const mmr_sho* h, double* kbase) {
+    return guarded([&] {
+        MMR_REQUIRE(h && kbase, "NULL argument");
+        const ShoPlan* s = reinterpret_cast<const ShoPlan*>(h);
+        if (s->base) s = s->base;   // setPhiDiv keeps the base encoding's kbase (sampHighOrder.m:590-622)
+        MMR_REQUIRE(!s->interp, "kbase is not formed by the interpolated approach");
+        const long long V = s->V, M = s->M;
+        // sample chunks of at most 32 Mi values (256 MiB) through one device buffer
+        const long long nm_max = std::max<long long>(1, std::min<long long>(M, (32LL << 20) / std::max<long long>(V, 1)));
+        DevBuf buf;
+        buf.ensure((size_t)V * nm_max * sizeof(double));
+        for (long long m0 = 0; m0 < M; m0 += nm_max) {
+            const long long nm = std::min(nm_max, M - m0);
+            sho_kbase_kernel<<<(unsigned)cdiv(V * nm, 256), 256>>>(s->d_B.as<double>(), s->d_P.as<double>(), s->K, V, M,
+                                                                   m0, nm, buf.as<double>());
+            check_launch("sho_kbase");
+            MMR_CUDA(cudaMemcpy(kbase + (size_t)V * m0, buf.p, (size_t)V * nm * sizeof(double), cudaMemcpyDeviceToHost));
+        }
     });
 }
 

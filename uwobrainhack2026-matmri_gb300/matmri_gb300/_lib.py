@@ -122,6 +122,7 @@ SIGNATURES = {
     "mmr_sho_apply": (C.c_int, [C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]),
     "mmr_sho_destroy": (C.c_int, [C.c_void_p]),
     "mmr_sho_set_tensor": (C.c_int, [C.c_void_p, C.c_int]),
+    "mmr_sho_kbase": (C.c_int, [C.c_void_p, C.c_void_p]),
     "mmr_sho_interp_create": (C.c_int, [C.POINTER(ShoInterpDesc), C.POINTER(C.c_void_p)]),
     "mmr_dense_normal": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int64), C.c_int64, C.c_void_p,
                                    C.c_void_p]),

@@ -338,6 +338,16 @@ class sampHighOrder(_Op):
         return self
 
     @property
+    def kbase(self):
+        """The FP64 encoding phase [V x M] of a direct plan (prepForDirect, sampHighOrder.m:496-588; the
+        matrix operators/mrSampFuncMat.m:35 reads), evaluated on the device from the plan's basis."""
+        if self.approach == 1:
+            raise AttributeError("kbase is not formed by the interpolated approach")
+        out = np.empty((self.V, self.M), dtype=np.float64, order="F")
+        _lib.check(_lib.load().mmr_sho_kbase(self.handle, out.ctypes.data))
+        return out
+
+    @property
     def handle(self):
         return self._h.ptr
 

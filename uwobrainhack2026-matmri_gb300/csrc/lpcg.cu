@@ -110,36 +110,33 @@ __global__ void lp_init_kernel(const float2* __restrict__ b, const float2* __res
     }
 }
 
-// q += tik.*p ; p'q ; p'r ; (p, q) into the ring slot of this iteration
-__global__ void lp_pq_kernel(const float2* __restrict__ p, float2* __restrict__ q, const float2* __restrict__ r,
-                             const float* __restrict__ tik, float2* __restrict__ ring_p, float2* __restrict__ ring_q,
+// q += tik.*p ; p'q.  Only when the normal operator cannot accumulate p'q in its last kernel
+// (sense_normal_dot): p'r comes from lp_p, the ring copies from lp_update and lp_p.
+__global__ void lp_pq_kernel(const float2* __restrict__ p, float2* __restrict__ q, const float* __restrict__ tik,
                              long long n, LpState* st) {
     if (st->finished) return;
-    const long long so = (long long)st->slot * n;
-    double v[4] = {0, 0, 0, 0};
+    double v[2] = {0, 0};
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-        const float2 pi = p[i], ri = r[i];
+        const float2 pi = p[i];
         float2 qi = q[i];
         if (tik) {
             qi = make_float2(qi.x + tik[i] * pi.x, qi.y + tik[i] * pi.y);
             q[i] = qi;
         }
-        ring_p[so + i] = pi;
-        ring_q[so + i] = qi;
         v[0] += (double)pi.x * qi.x + (double)pi.y * qi.y;
         v[1] += (double)pi.x * qi.y - (double)pi.y * qi.x;
-        v[2] += (double)pi.x * ri.x + (double)pi.y * ri.y;
-        v[3] += (double)pi.x * ri.y - (double)pi.y * ri.x;
     }
-    double* const dst[4] = {&st->pq_re, &st->pq_im, &st->pr_re, &st->pr_im};
-    block_accumulate<4>(v, dst);
+    double* const dst[2] = {&st->pq_re, &st->pq_im};
+    block_accumulate<2>(v, dst);
 }
 
-// x += alpha p ; r -= alpha q ; |r|^2 ; |x - gt|^2 ; history, stopping and stall tests
+// x += alpha p ; r -= alpha q ; q into the ring slot of this iteration ; |r|^2 ; |x - gt|^2 ;
+// history, stopping and stall tests
 __global__ void lp_update_kernel(float2* __restrict__ x, const float2* __restrict__ p, const float2* __restrict__ q,
-                                 float2* __restrict__ r, const float2* __restrict__ gt, long long n, LpState* st,
-                                 double* hist) {
+                                 float2* __restrict__ r, float2* __restrict__ ring_q, const float2* __restrict__ gt,
+                                 long long n, LpState* st, double* hist) {
     if (st->finished) return;
+    float2* __restrict__ rq = ring_q + (long long)st->slot * n;
     // a direction without curvature (p = 0, or a non-finite network output) takes no step;
     // the finalize below then reports a stall so that the host falls back to plain CG
     const double pqr = st->pq_re, pqi = st->pq_im;
@@ -149,8 +146,10 @@ __global__ void lp_update_kernel(float2* __restrict__ x, const float2* __restric
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const float2 xo = x[i], ro = r[i];
         float2 xn = xo, rn = ro;
+        const float2 qi = q[i];
+        rq[i] = qi;
         if (!bad) {
-            const float2 pi = p[i], qi = q[i];
+            const float2 pi = p[i];
             xn = make_float2((float)((double)xo.x + al.x * pi.x - al.y * pi.y),
                              (float)((double)xo.y + al.x * pi.y + al.y * pi.x));
             rn = make_float2((float)((double)ro.x - (al.x * qi.x - al.y * qi.y)),
@@ -254,12 +253,15 @@ __global__ void lp_qz_kernel(const float2* __restrict__ ring_q, const float2* __
     }
 }
 
-// p = z + sum_j beta_j p_j over the valid ring slots (z = r after the switch to plain CG)
+// p = z + sum_j beta_j p_j over the valid ring slots (z = r after the switch to plain CG); p into
+// the ring slot of the next iteration; p'r for the next step length
 __global__ void lp_p_kernel(float2* __restrict__ p, const float2* __restrict__ zn, const float2* __restrict__ r,
-                            const float2* __restrict__ ring_p, long long n, const LpState* st) {
+                            float2* __restrict__ ring_p, long long n, LpState* st) {
     if (st->finished) return;
     const float2* __restrict__ z = st->plain ? r : zn;
     const int nv = st->nstored;
+    float2* __restrict__ rp = ring_p + (long long)st->slot * n;
+    double d[2] = {0, 0};
     double br[LP_MAXM], bi[LP_MAXM];
 #pragma unroll
     for (int j = 0; j < LP_MAXM; ++j) {
@@ -277,8 +279,15 @@ __global__ void lp_p_kernel(float2* __restrict__ p, const float2* __restrict__ z
                 ay += br[j] * pj.y + bi[j] * pj.x;
             }
         }
-        p[i] = make_float2((float)ax, (float)ay);
+        const float2 pn = make_float2((float)ax, (float)ay);
+        const float2 ri = r[i];
+        p[i] = pn;
+        rp[i] = pn;
+        d[0] += (double)pn.x * ri.x + (double)pn.y * ri.y;
+        d[1] += (double)pn.x * ri.y - (double)pn.y * ri.x;
     }
+    double* const dst[2] = {&st->pr_re, &st->pr_im};
+    block_accumulate<2>(d, dst);
 }
 
 // |v|^2 into *out (zeroed by the caller)
@@ -312,11 +321,14 @@ static void lp_iter(const LpCall& c, LpWorkspace& w, bool learned, cudaStream_t 
     const float* tik = c.has_tik ? w.tik.as<float>() : nullptr;
     float2* ring_p = w.ring_p.as<float2>();
     float2* ring_q = w.ring_q.as<float2>();
-    sense_normal(*c.a, p, q, st, &sp->finished);
-    lp_pq_kernel<<<g, 256, 0, st>>>(p, q, r, tik, ring_p, ring_q, n, sp);
-    check_launch("lp_pq");
-    lp_update_kernel<<<g, 256, 0, st>>>(w.x.as<float2>(), p, q, r, c.has_gt ? w.gt.as<float2>() : nullptr, n, sp,
-                                        w.hist.as<double>());
+    // q = H p with p'q accumulated in the normal operator's coil sum when it is the last kernel
+    if (!sense_normal_dot(*c.a, p, q, tik, &sp->pq_re, st, &sp->finished)) {
+        sense_normal(*c.a, p, q, st, &sp->finished);
+        lp_pq_kernel<<<g, 256, 0, st>>>(p, q, tik, n, sp);
+        check_launch("lp_pq");
+    }
+    lp_update_kernel<<<g, 256, 0, st>>>(w.x.as<float2>(), p, q, r, ring_q, c.has_gt ? w.gt.as<float2>() : nullptr,
+                                        n, sp, w.hist.as<double>());
     check_launch("lp_update");
     if (learned) cnn_forward(*c.net, r, z, c.nx, c.ny, 1, &sp->rr, c.flags, st);
     lp_qz_kernel<<<g, 256, 0, st>>>(ring_q, z, r, n, sp);
@@ -373,13 +385,12 @@ static void lp_start(const LpCall& c, LpWorkspace& w, bool learned, bool have_x,
                                       c.has_gt ? w.gt.as<float2>() : nullptr, w.r.as<float2>(), n, sp,
                                       w.hist.as<double>(), 0);
     check_launch("lp_init");
-    if (learned) {
-        cnn_forward(*c.net, w.r.as<float2>(), w.z.as<float2>(), c.nx, c.ny, 1, &sp->rr, c.flags, st);
-        MMR_CUDA(cudaMemcpyAsync(w.p.p, w.z.p, n * 8, cudaMemcpyDeviceToDevice, st));
-    } else {
-        MMR_CUDA(cudaMemcpyAsync(w.p.p, w.r.p, n * 8, cudaMemcpyDeviceToDevice, st));
-    }
+    if (learned) cnn_forward(*c.net, w.r.as<float2>(), w.z.as<float2>(), c.nx, c.ny, 1, &sp->rr, c.flags, st);
     MMR_CUDA(cudaMemsetAsync(w.state.p, 0, LP_ACC_BYTES, st));
+    // p = z (r for plain CG; no stored directions yet), its ring slot 0 and p'r
+    lp_p_kernel<<<g, 256, 0, st>>>(w.p.as<float2>(), learned ? w.z.as<float2>() : w.r.as<float2>(), w.r.as<float2>(),
+                                   w.ring_p.as<float2>(), n, sp);
+    check_launch("lp_p");
 }
 
 static void lp_solve(SenseOp& a, const void* y_user, CnnNet* net, const void* x0_user, const mmr_lpcg_opts& o,

@@ -211,26 +211,31 @@ __global__ void cg_update_kernel(float2* __restrict__ x, const float2* __restric
     const double rso = st->res_sq_old, ar = st->pAp_re, ai = st->pAp_im;
     const double den = ar * ar + ai * ai;
     const double alr = rso * ar / den, ali = -rso * ai / den;     // res_sq_old / (p' Ap)
+    // The vector updates run as FP32 FMAs with alpha rounded once (the vectors are complex64); the
+    // norms take FP32 squares of each element (positive terms: no cancellation) summed in FP64.
+    // |x|^2 and |x - xold|^2 only when a history or a stopping rule needs them (cgne.m:101-108).
+    const float fr = (float)alr, fi = (float)ali;
+    const bool fxn = st->findxnorm, fxd = st->findxdiff;
     double v[4] = {0, 0, 0, 0};
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const float2 pi = p[i];
         const float2 xo = x[i];
-        const float2 xn = make_float2((float)((double)xo.x + alr * pi.x - ali * pi.y),
-                                      (float)((double)xo.y + alr * pi.y + ali * pi.x));
+        const float2 xn = make_float2(fmaf(fr, pi.x, fmaf(-fi, pi.y, xo.x)), fmaf(fr, pi.y, fmaf(fi, pi.x, xo.y)));
         x[i] = xn;
-        const double dx = (double)xn.x - xo.x, dy = (double)xn.y - xo.y;
-        v[1] += (double)xn.x * xn.x + (double)xn.y * xn.y;
-        v[2] += dx * dx + dy * dy;
+        if (fxn) v[1] += (double)fmaf(xn.x, xn.x, xn.y * xn.y);
+        if (fxd) {
+            const float dx = xn.x - xo.x, dy = xn.y - xo.y;
+            v[2] += (double)fmaf(dx, dx, dy * dy);
+        }
         if (gt) {
             const double ex = (double)gt[i].x - xn.x, ey = (double)gt[i].y - xn.y;
             v[3] += ex * ex + ey * ey;
         }
         if (MODE == 0) {
             const float2 a = Ap[i], r = res[i];
-            const float2 rn = make_float2((float)((double)r.x - (alr * a.x - ali * a.y)),
-                                          (float)((double)r.y - (alr * a.y + ali * a.x)));
+            const float2 rn = make_float2(fmaf(-fr, a.x, fmaf(fi, a.y, r.x)), fmaf(-fr, a.y, fmaf(-fi, a.x, r.y)));
             res[i] = rn;
-            v[0] += (double)rn.x * rn.x + (double)rn.y * rn.y;
+            v[0] += (double)fmaf(rn.x, rn.x, rn.y * rn.y);
         }
     }
     double* const dst[4] = {MODE == 0 ? &st->acc_res : nullptr, &st->acc_xn, &st->acc_xd, &st->acc_mse};
@@ -265,10 +270,10 @@ __global__ void cg_p_kernel(float2* __restrict__ p, const float2* __restrict__ r
     // runs after the finalize of the same iteration: skip only if finished *before* it
     pdl_wait();
     pdl_trigger();
-    const double beta = st->beta;
+    const float beta = (float)st->beta;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const float2 r = res[i], pi = p[i];
-        p[i] = make_float2((float)((double)r.x + beta * pi.x), (float)((double)r.y + beta * pi.y));
+        p[i] = make_float2(fmaf(beta, pi.x, r.x), fmaf(beta, pi.y, r.y));
     }
 }
 
@@ -385,7 +390,7 @@ struct CgRun {
 // Set-up of one solve on the operator's stream (ordered after `ust`): inputs, b = A'(W.*y),
 // x0, the options in the device state, the initial residual (cgne.m:135-207).
 static CgRun cg_begin(SenseOp& a, const void* b_user, const void* x0_user, const float* W, const mmr_cgne_opts& o,
-                      cudaStream_t ust) {
+                      bool hist_out, cudaStream_t ust) {
     CgRun run;
     if (!a.solver_ws) a.solver_ws = new CgWorkspace();
     CgWorkspace& w = *static_cast<CgWorkspace*>(a.solver_ws);
@@ -435,8 +440,11 @@ static CgRun cg_begin(SenseOp& a, const void* b_user, const void* x0_user, const
     h.stopOnResInc = o.stop_on_res_inc;
     h.stopOnXdifInc = o.stop_on_xdif_inc;
     h.nseExtraIt = o.nse_extra_it;
-    h.findxnorm = 1;                                   // nargout > 3 (histories requested)
-    h.findxdiff = 1;
+    // cgne.m:101-108: |x|^2 when histories are returned (nargout > 3) or xChangeThresh is set; |dx|^2
+    // also for stopOnXdifInc
+    const bool want_hist = hist_out && o.want_history;
+    h.findxnorm = want_hist || h.has_xChange;
+    h.findxdiff = want_hist || h.has_xChange || h.stopOnXdifInc > 0;
     h.has_gt = has_gt;
     h.cap = cap;
     h.nitmax = nitmax0;
@@ -532,7 +540,7 @@ static void cg_end(SenseOp& a, CgRun& run, void* x_user, mmr_cgne_hist* hist, cu
 
 static void cg_solve(SenseOp& a, const void* b_user, const void* x0_user, const float* W, const mmr_cgne_opts& o,
                      void* x_user, mmr_cgne_hist* hist, cudaStream_t ust) {
-    CgRun run = cg_begin(a, b_user, x0_user, W, o, ust);
+    CgRun run = cg_begin(a, b_user, x0_user, W, o, hist != nullptr, ust);
     CgWorkspace& w = *static_cast<CgWorkspace*>(a.solver_ws);
     cudaStream_t st = a.stream;
     CgState* sp = w.state.as<CgState>();
@@ -606,7 +614,7 @@ static void cg_solve_batch(SenseOp* const* ops, int nops, const void* const* b_u
             if (runs[i].ev) cudaEventDestroy(runs[i].ev);
     };
     try {
-        for (int i = 0; i < nops; ++i) runs.push_back(cg_begin(*ops[i], b_user[i], nullptr, nullptr, o, ust));
+        for (int i = 0; i < nops; ++i) runs.push_back(cg_begin(*ops[i], b_user[i], nullptr, nullptr, o, hists != nullptr, ust));
         MMR_CUDA(cudaStreamCreateWithFlags(&origin, cudaStreamNonBlocking));
         evs.resize(nops + 1);
         for (auto& e : evs) MMR_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));

@@ -142,6 +142,8 @@ __global__ void lp_update_kernel(float2* __restrict__ x, const float2* __restric
     const double pqr = st->pq_re, pqi = st->pq_im;
     const bool bad = !(pqr * pqr + pqi * pqi > 0.0) || !isfinite(pqr + pqi + st->pr_re + st->pr_im);
     const double2 al = bad ? make_double2(0.0, 0.0) : cdiv_d(st->pr_re, st->pr_im, pqr, pqi);
+    // FP32 FMAs with alpha rounded once (complex64 vectors); |r|^2 from FP32 squares summed in FP64
+    const float ar = (float)al.x, ai = (float)al.y;
     double v[2] = {0, 0};
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const float2 xo = x[i], ro = r[i];
@@ -150,14 +152,12 @@ __global__ void lp_update_kernel(float2* __restrict__ x, const float2* __restric
         rq[i] = qi;
         if (!bad) {
             const float2 pi = p[i];
-            xn = make_float2((float)((double)xo.x + al.x * pi.x - al.y * pi.y),
-                             (float)((double)xo.y + al.x * pi.y + al.y * pi.x));
-            rn = make_float2((float)((double)ro.x - (al.x * qi.x - al.y * qi.y)),
-                             (float)((double)ro.y - (al.x * qi.y + al.y * qi.x)));
+            xn = make_float2(fmaf(ar, pi.x, fmaf(-ai, pi.y, xo.x)), fmaf(ar, pi.y, fmaf(ai, pi.x, xo.y)));
+            rn = make_float2(fmaf(-ar, qi.x, fmaf(ai, qi.y, ro.x)), fmaf(-ar, qi.y, fmaf(-ai, qi.x, ro.y)));
             x[i] = xn;
             r[i] = rn;
         }
-        v[0] += (double)rn.x * rn.x + (double)rn.y * rn.y;
+        v[0] += (double)fmaf(rn.x, rn.x, rn.y * rn.y);
         if (gt) {
             const double dx = (double)gt[i].x - xn.x, dy = (double)gt[i].y - xn.y;
             v[1] += dx * dx + dy * dy;
@@ -262,24 +262,25 @@ __global__ void lp_p_kernel(float2* __restrict__ p, const float2* __restrict__ z
     const int nv = st->nstored;
     float2* __restrict__ rp = ring_p + (long long)st->slot * n;
     double d[2] = {0, 0};
-    double br[LP_MAXM], bi[LP_MAXM];
+    // the combination in FP32 FMAs with the FP64 betas rounded once (p is complex64)
+    float br[LP_MAXM], bi[LP_MAXM];
 #pragma unroll
     for (int j = 0; j < LP_MAXM; ++j) {
-        br[j] = st->beta[2 * j];
-        bi[j] = st->beta[2 * j + 1];
+        br[j] = (float)st->beta[2 * j];
+        bi[j] = (float)st->beta[2 * j + 1];
     }
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
         const float2 zi = z[i];
-        double ax = zi.x, ay = zi.y;
+        float ax = zi.x, ay = zi.y;
 #pragma unroll
         for (int j = 0; j < LP_MAXM; ++j) {
             if (j < nv) {
                 const float2 pj = ring_p[(long long)j * n + i];
-                ax += br[j] * pj.x - bi[j] * pj.y;
-                ay += br[j] * pj.y + bi[j] * pj.x;
+                ax = fmaf(br[j], pj.x, fmaf(-bi[j], pj.y, ax));
+                ay = fmaf(br[j], pj.y, fmaf(bi[j], pj.x, ay));
             }
         }
-        const float2 pn = make_float2((float)ax, (float)ay);
+        const float2 pn = make_float2(ax, ay);
         const float2 ri = r[i];
         p[i] = pn;
         rp[i] = pn;

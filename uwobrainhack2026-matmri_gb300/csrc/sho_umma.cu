@@ -23,10 +23,13 @@
 // (16 producer warps for up to 16 coils per pass, 8 for 32):
 //   producers   per stage (32 inputs x 128 rows) read the phase tile from
 //               shared memory, evaluate sincos on the SFU, split to FP16 hi/lo
-//               and store the A operand in the no-swizzle K-major UMMA layout;
-//               thread 0 also bulk-copies the stage's B operand;
-//   TMA warp    cp.async.bulk.tensor of the phase tiles into a 4-deep ring,
-//               each tile prefetched into L2 twelve stages ahead;
+//               and store the A operand in the no-swizzle K-major UMMA layout
+//               (a 2-deep ring);
+//   TMA warp    cp.async.bulk.tensor of the phase tiles into an 8-deep ring
+//               (6 for 32-coil groups), each tile prefetched into L2 twelve
+//               stages ahead;
+//   B loader    one bulk copy per stage of the pre-split coil data into a
+//               4-deep ring that the MMA thread releases;
 //   MMA warp    one thread issues tcgen05.mma (kind::f16, M 128, K 16),
 //               commits stage completion to the operand ring's mbarriers and
 //               chunk completion to its own, and after seeing a chunk complete
@@ -37,6 +40,9 @@
 //               (each its 32-lane quarter) read the finished set with
 //               tcgen05.ld and add it to FP32 register totals, which they store
 //               as the item's partial sums at its end.
+// Generic stores into an A slot that MMAs read through the async proxy follow
+// a fence.proxy.async after the slot's release; without it, adjoint rows came
+// out wrong on a GB300.
 // The B operand stacks hi and lo rows, so per 16 inputs and per cos / sin part
 // two MMAs cover the three products: A_hi x [B_hi; B_lo] (N = 2 N0: main and
 // the first correction) and A_lo x B_hi (N = N0: the second correction).  A
@@ -61,8 +67,8 @@ namespace umma {
 
 constexpr int BM = 128;                      // output rows per work item (TMEM lanes)
 constexpr int KS = 32;                       // inputs per pipeline stage
-constexpr int ST = 4;                        // phase-tile ring depth
-constexpr int SA = 3;                        // A/B operand ring depth
+constexpr int SA = 2;                        // A operand ring depth
+constexpr int SB = 4;                        // B operand ring depth
 constexpr int PS = 2;                        // stages per TMEM accumulation set (64 inputs)
 constexpr int PF = 12;                       // L2 prefetch distance of the phase tiles, in stages
 constexpr int TURN_BYTES = BM * KS * 4;      // 16 KB
@@ -74,9 +80,13 @@ constexpr float LO_SCALE = 2048.f;
 constexpr float ROUND_MAGIC = 12582912.f;    // 1.5 * 2^23: x + m - m rounds |x| < 2^22 to an integer
 constexpr uint32_t WAIT_POLLS = 1u << 22;
 
-// warps 0 .. NPW-1 producers, NPW the TMA warp, NPW+1 the MMA warp, NPW+2 .. NPW+5 the epilogue
+// warps 0 .. NPW-1 producers, NPW the TMA warp (phase tiles), NPW+1 the MMA warp, NPW+2 the B loader,
+// NPW+3 .. NPW+6 the epilogue
 __host__ __device__ constexpr int nprod_warps(int N0) { return N0 <= 32 ? 16 : 8; }
-__host__ __device__ constexpr int nthreads(int N0) { return (nprod_warps(N0) + 6) * 32; }
+__host__ __device__ constexpr int nthreads(int N0) { return (nprod_warps(N0) + 7) * 32; }
+// phase-tile ring depth: as many 16 KB tiles in flight as shared memory leaves (HBM latency x
+// bandwidth per SM is about 90 KB)
+__host__ __device__ constexpr int n_turn_stages(int N0) { return N0 <= 32 ? 8 : 6; }
 // B operand of one stage: a cos and a sin sub-tile, each [KS / 8][2 N0 rows: hi then lo][8] halves
 __host__ __device__ constexpr int b_sub_bytes(int N0) { return 2 * N0 * KS * 2; }
 __host__ __device__ constexpr int b_bytes(int N0) { return 2 * b_sub_bytes(N0); }
@@ -86,15 +96,14 @@ __host__ __device__ constexpr int nsets(int N0) {
     return TMEM_COLS / set_w(N0) < MAX_SETS ? TMEM_COLS / set_w(N0) : MAX_SETS;
 }
 
-struct Smem {        // offsets in the 1024-aligned dynamic shared memory
-    static constexpr int turn = 0;
-    static constexpr int a = turn + ST * TURN_BYTES;
-    static constexpr int b = a + SA * A_BYTES;
-};
-__host__ __device__ constexpr int bar_off(int N0) { return Smem::b + SA * b_bytes(N0); }
-// barriers: tfull[ST] tempty[ST] afull[SA] bfull[SA] aempty[SA] setfull[MAX_SETS] setempty[MAX_SETS] drain
-// chunk[2], then the TMEM address slot
-__host__ __device__ constexpr int nbars() { return 2 * ST + 3 * SA + 2 * MAX_SETS + 3; }
+// offsets in the 1024-aligned dynamic shared memory: phase tiles, A stages, B stages, barriers
+__host__ __device__ constexpr int off_a(int N0) { return n_turn_stages(N0) * TURN_BYTES; }
+__host__ __device__ constexpr int off_b(int N0) { return off_a(N0) + SA * A_BYTES; }
+__host__ __device__ constexpr int bar_off(int N0) { return off_b(N0) + SB * b_bytes(N0); }
+// barriers: tfull[ST] tempty[ST] afull[SA] aempty[SA] bfull[SB] bempty[SB] setfull[MAX_SETS]
+// setempty[MAX_SETS] drain chunk[2], then the TMEM address slot
+constexpr int MAX_ST = 8;
+__host__ __device__ constexpr int nbars() { return 2 * MAX_ST + 2 * SA + 2 * SB + 2 * MAX_SETS + 3; }
 __host__ __device__ constexpr int smem_bytes(int N0) { return bar_off(N0) + nbars() * 8 + 16 + 1024; }
 
 __device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -215,7 +224,9 @@ __global__ void __launch_bounds__(umma::nthreads(N0), 1)
     constexpr int NS = nsets(N0);
     constexpr int SW = set_w(N0);
     constexpr int NPW = nprod_warps(N0), NPROD = NPW * 32;
-    constexpr int WARP_TMA = NPW, WARP_MMA = NPW + 1;
+    constexpr int WARP_TMA = NPW, WARP_MMA = NPW + 1, WARP_B = NPW + 2;
+    constexpr int ST = n_turn_stages(N0);
+    constexpr int OFF_A = off_a(N0), OFF_B = off_b(N0);
     constexpr int CPT = (BM * KS / 8) / NPROD;     // 8-input chunks per producer thread and stage
     if (active && *active) return;
     extern __shared__ uint8_t smem_raw[];
@@ -223,14 +234,16 @@ __global__ void __launch_bounds__(umma::nthreads(N0), 1)
     const uint32_t s0 = su32(sm);
     const uint32_t bars = s0 + bar_off(N0);
     auto tfull = [&](int i) { return bars + 8u * i; };
-    auto tempty = [&](int i) { return bars + 8u * (ST + i); };
-    auto afull = [&](int i) { return bars + 8u * (2 * ST + i); };
-    auto bfull = [&](int i) { return bars + 8u * (2 * ST + SA + i); };
-    auto aempty = [&](int i) { return bars + 8u * (2 * ST + 2 * SA + i); };
-    auto setfull = [&](int i) { return bars + 8u * (2 * ST + 3 * SA + i); };
-    auto setempty = [&](int i) { return bars + 8u * (2 * ST + 3 * SA + MAX_SETS + i); };
-    const uint32_t drain = bars + 8u * (2 * ST + 3 * SA + 2 * MAX_SETS);
-    auto chunkbar = [&](int i) { return bars + 8u * (2 * ST + 3 * SA + 2 * MAX_SETS + 1 + i); };
+    auto tempty = [&](int i) { return bars + 8u * (MAX_ST + i); };
+    auto afull = [&](int i) { return bars + 8u * (2 * MAX_ST + i); };
+    auto aempty = [&](int i) { return bars + 8u * (2 * MAX_ST + SA + i); };
+    auto bfull = [&](int i) { return bars + 8u * (2 * MAX_ST + 2 * SA + i); };
+    auto bempty = [&](int i) { return bars + 8u * (2 * MAX_ST + 2 * SA + SB + i); };
+    constexpr int SET0 = 2 * MAX_ST + 2 * SA + 2 * SB;
+    auto setfull = [&](int i) { return bars + 8u * (SET0 + i); };
+    auto setempty = [&](int i) { return bars + 8u * (SET0 + MAX_SETS + i); };
+    const uint32_t drain = bars + 8u * (SET0 + 2 * MAX_SETS);
+    auto chunkbar = [&](int i) { return bars + 8u * (SET0 + 2 * MAX_SETS + 1 + i); };
     uint32_t* tslot = reinterpret_cast<uint32_t*>(sm + bar_off(N0) + nbars() * 8);
     __shared__ volatile int abort_flag;
 
@@ -243,8 +256,11 @@ __global__ void __launch_bounds__(umma::nthreads(N0), 1)
         }
         for (int i = 0; i < SA; ++i) {
             bar_init(afull(i), NPROD);
-            bar_init(bfull(i), 1);
             bar_init(aempty(i), 1);
+        }
+        for (int i = 0; i < SB; ++i) {
+            bar_init(bfull(i), 1);
+            bar_init(bempty(i), 1);
         }
         for (int i = 0; i < NS; ++i) {
             bar_init(setfull(i), 1);
@@ -280,15 +296,10 @@ __global__ void __launch_bounds__(umma::nthreads(N0), 1)
                 const int ts = (int)(g % ST), as = (int)(g % SA);
                 if (!bar_wait(tfull(ts), (uint32_t)((g / ST) & 1), &abort_flag, err)) break;
                 if (g >= SA && !bar_wait(aempty(as), (uint32_t)(((g / SA) + 1) & 1), &abort_flag, err)) break;
-                if (tid == 0) {
-                    bar_expect(bfull(as), (uint32_t)b_bytes(N0));
-                    asm volatile(
-                        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                            s0 + Smem::b + as * b_bytes(N0)),
-                        "l"(bglob + (size_t)q * (b_bytes(N0) / 2)), "r"((uint32_t)b_bytes(N0)), "r"(bfull(as))
-                        : "memory");
-                }
-                const float* tile = reinterpret_cast<const float*>(sm + Smem::turn + ts * TURN_BYTES);
+                // the MMAs of this slot's previous use read it through the async proxy: order them
+                // before this thread's generic stores to it
+                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                const float* tile = reinterpret_cast<const float*>(sm + ts * TURN_BYTES);
                 float t[CPT][8];
 #pragma unroll
                 for (int j = 0; j < CPT; ++j) {
@@ -308,7 +319,7 @@ __global__ void __launch_bounds__(umma::nthreads(N0), 1)
                     }
                 }
                 bar_arrive(tempty(ts));
-                uint8_t* a = sm + Smem::a + as * A_BYTES;
+                uint8_t* a = sm + OFF_A + as * A_BYTES;
 #pragma unroll
                 for (int j = 0; j < CPT; ++j) {
                     const int kc = kq + j * (NPROD / BM);
@@ -341,11 +352,37 @@ __global__ void __launch_bounds__(umma::nthreads(N0), 1)
                 bar_arrive(afull(as));
             }
         }
-        // drain: the B copies this CTA issued must land before it exits
-        if (tid == 0 && abort_flag) {
-            for (long long k = std::max<long long>(0, g - SA); k < g; ++k)
-                bar_wait(bfull((int)(k % SA)), (uint32_t)((k / SA) & 1), &abort_flag, err, true);
+    } else if (warp == WARP_B) {
+        // -------------------------------------------------------------- B loader --
+        // the stage's B operand (coil data, FP16 hi / lo, both parts) by one bulk copy into a ring
+        // that the MMA thread releases stage by stage
+        long long g = 0;
+        if (lane == 0) {
+            for (long long w = blockIdx.x; w < nitems && !abort_flag; w += gridDim.x) {
+                long long rt, sp, qa, qb;
+                item_range(w, nsplit, Q, rt, sp, qa, qb);
+                bool ok = true;
+                for (long long q = qa; q < qb; ++q, ++g) {
+                    const int bs = (int)(g % SB);
+                    if (g >= SB && !bar_wait(bempty(bs), (uint32_t)(((g / SB) + 1) & 1), &abort_flag, err)) {
+                        ok = false;
+                        break;
+                    }
+                    bar_expect(bfull(bs), (uint32_t)b_bytes(N0));
+                    asm volatile(
+                        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                            s0 + OFF_B + bs * b_bytes(N0)),
+                        "l"(bglob + (size_t)q * (b_bytes(N0) / 2)), "r"((uint32_t)b_bytes(N0)), "r"(bfull(bs))
+                        : "memory");
+                }
+                if (!ok) break;
+            }
+            if (abort_flag) {   // the copies in flight land before the CTA exits
+                for (long long k = std::max<long long>(0, g - SB); k < g; ++k)
+                    bar_wait(bfull((int)(k % SB)), (uint32_t)((k / SB) & 1), &abort_flag, err, true);
+            }
         }
+        __syncwarp();
     } else if (warp == WARP_TMA) {
         // ------------------------------------------------------------------ TMA --
         // Each phase tile is also prefetched into L2 PF stages before its load, so that the
@@ -390,7 +427,7 @@ __global__ void __launch_bounds__(umma::nthreads(N0), 1)
                     const int cy = ADJ ? (int)(rt * BM) : (int)(q * KS);    // voxels
                     asm volatile(
                         "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, "
-                        "{%2, %3}], [%4];" ::"r"(s0 + Smem::turn + ts * TURN_BYTES),
+                        "{%2, %3}], [%4];" ::"r"(s0 + ts * TURN_BYTES),
                         "l"(&turn_map), "r"(cx), "r"(cy), "r"(tfull(ts))
                         : "memory");
                     prefetch_next();
@@ -437,15 +474,15 @@ __global__ void __launch_bounds__(umma::nthreads(N0), 1)
                     const uint32_t dset = tmem + (uint32_t)(set * SW);
                     const long long q1 = std::min<long long>(q0 + PS, qb);
                     for (long long q = q0; q < q1; ++q, ++g) {
-                        const int as = (int)(g % SA);
-                        const uint32_t par = (uint32_t)((g / SA) & 1);
-                        if (!bar_wait(afull(as), par, &abort_flag, err) || !bar_wait(bfull(as), par, &abort_flag, err)) {
+                        const int as = (int)(g % SA), bs = (int)(g % SB);
+                        if (!bar_wait(bfull(bs), (uint32_t)((g / SB) & 1), &abort_flag, err) ||
+                            !bar_wait(afull(as), (uint32_t)((g / SA) & 1), &abort_flag, err)) {
                             ok = false;
                             break;
                         }
                         fence_after();
-                        const uint32_t a0 = s0 + Smem::a + as * A_BYTES;
-                        const uint32_t b0 = s0 + Smem::b + as * b_bytes(N0);
+                        const uint32_t a0 = s0 + OFF_A + as * A_BYTES;
+                        const uint32_t b0 = s0 + OFF_B + bs * b_bytes(N0);
 #pragma unroll
                         for (int j = 0; j < KS / 16; ++j) {
                             const uint32_t ao = j * 2 * LBO_A, bo = j * 2 * LBO_B;
@@ -462,6 +499,7 @@ __global__ void __launch_bounds__(umma::nthreads(N0), 1)
                             mma(dset + 2 * N0, asl, bs, ID1, 1u);
                         }
                         commit(aempty(as));
+                        commit(bempty(bs));
                     }
                     if (!ok) break;
                     commit(chunkbar((int)(c & 1)));

@@ -89,10 +89,10 @@ def test_highorder_workload_small(mm):
 @pytest.mark.parametrize("shape", [((24, 20), 1500), ((32, 32), 1024), ((20, 18), 1501)])
 def test_tensor_core_contraction(mm, ncoil, shape):
     """The tensor-core paths (FP16 hi + scaled lo splits, FP32 accumulation) against the FP64
-    restatement and the SIMT path, both directions: the tcgen05 kernel (default; 1501 samples are
-    not a multiple of the 4-float TMA pitch, so that plan runs the mma.sync kernel instead) and the
-    mma.sync kernel, coil counts across the coil-group widths (8, 16, 32 and two groups of 32) and
-    sizes that are not multiples of the 32-input stage or the 128-row tile."""
+    restatement and the SIMT path, both directions: the tcgen05 kernel (default; it reads a
+    zero-padded blocked copy of the table, so 1501 samples need no special case) and the mma.sync
+    kernel, coil counts across the coil-group widths (8, 16, 32 and two groups of 32) and sizes that
+    are not multiples of the 32-input stage, the 128-row tile or the 4-stage phase block."""
     from matmri_gb300 import synth
     imN, M = shape
     b0, t, spha, conc, grid = synth.highorder_inputs(N=imN[0], M=M, seed=11)

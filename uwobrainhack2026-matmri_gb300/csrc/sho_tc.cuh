@@ -1,8 +1,6 @@
 // Tensor-core path of the sampHighOrder encoding (sho_tc.cu).
 #pragma once
 
-#include <cuda.h>
-
 #include "common.h"
 
 namespace mmr {
@@ -24,8 +22,8 @@ void sho_tc_alloc(ShoTcScratch& s, long long V, long long M);
 // tcgen05 path (sho_umma.cu): TMA tensor maps of the phase table and the device scratch of one plan.
 struct ShoUmma {
     bool ok = false;
-    CUtensorMap map_fwd;    // box {128 samples, 32 voxels}
-    CUtensorMap map_adj;    // box {32 samples, 128 voxels}, 128-byte swizzle
+    DevBuf tblk;            // the phase table in 128 x 128 blocks [V / 128][M / 128][128][128]
+    long long mblk = 0;     // blocks along M
     DevBuf b;               // B operand per stage (largest coil group), FP16 hi / lo
     DevBuf partial;         // split-K partial sums [nsplit][rows][2 coils]
     DevBuf cmax;            // per-column max |re|, |im|
@@ -33,8 +31,8 @@ struct ShoUmma {
     int nsplit[2] = {1, 1};   // forward, adjoint
     int* err = nullptr;       // device error word
 };
-// Builds the tensor maps and scratch; false when the table's shape does not suit the TMA
-// tiling (sample count not a multiple of 4) or the device is not an sm_10x part.
+// Builds the blocked phase table and scratch; false when the blocked copy does not fit in half of
+// the free device memory or the device is not an sm_10x part.
 bool sho_umma_prepare(ShoUmma& u, const float* turn, long long V, long long M);
 void sho_umma_forward(ShoUmma& u, long long V, long long M, const float2* x, float2* y, long long nb, cudaStream_t st,
                       const int* active);

@@ -1,5 +1,5 @@
 // sampHighOrder encoding on the 5th-generation tensor cores (tcgen05.mma, TMEM
-// accumulators, TMA-fed phase tiles).
+// accumulators, bulk-copied B operand, L2-prefetched phase table).
 //
 // Forward  y[m, c] = sum_v exp(+i 2 pi t[v, m]) x[v, c] / sqrt(V)   (sampHighOrder.m:376, 387)
 // adjoint  x[v, c] = sum_m exp(-i 2 pi t[v, m]) y[m, c] / sqrt(V)   (sampHighOrder.m:371, 387)
@@ -11,27 +11,28 @@
 //   forward  Bc = [ x_r ; x_i ]   Bs = [ -x_i ; x_r ]
 //   adjoint  Bc = [ y_r ; y_i ]   Bs = [  y_i ; -y_r ]
 // Precision: cos and sin are split in fixed point, hi = round(2^11 v) (an
-// integer, exact in FP16) and lo = 2^11 (2^11 v - hi); the column-normalised
-// coil data in floating point, hi = FP16(b), lo = FP16(2^11 (b - hi)).  TMEM
-// accumulators take hi*hi (main) and hi*lo, lo*hi (two corrections) in FP32,
-// combined as main + (corr1 + corr2) / 2^11 (about 22-bit operands).  Every
+// integer, exact in FP16) and lo = 2^11 v - hi (|lo| <= 1/2, FP16); the
+// column-normalised coil data in floating point, hi = FP16(b), lo = FP16(2^11
+// (b - hi)).  TMEM accumulators take hi*hi (main), hi*lo_b (corr1) and
+// lo_a*hi (corr2) in FP32, combined as main + corr1 / 2^11 + corr2 (about
+// 22-bit operands).  The phase comes from a blocked copy of the table in
+// radians, so the producers feed it straight to the SFU.  Every
 // accumulation in TMEM covers 64 inputs; the epilogue adds the accumulation
 // sets in FP32 registers and the split-K partials are summed in FP64 in a
 // fixed order by a second kernel.
 //
 // One persistent CTA per SM walks (row tile, K split) work items; warp roles
 // (16 producer warps for up to 16 coils per pass, 8 for 32):
-//   producers   per stage (32 inputs x 128 rows) read the phase tile from
-//               shared memory, evaluate sincos on the SFU, split to FP16 hi/lo
-//               and store the A operand in the no-swizzle K-major UMMA layout
-//               (a 2-deep ring);
-//   TMA warp    cp.async.bulk.tensor of the phase tiles into an 8-deep ring
-//               (6 for 32-coil groups), each tile prefetched into L2 twelve
-//               stages ahead;
+//   producers   per stage (32 inputs x 128 rows) load their phases straight
+//               from global memory one stage ahead, into registers (thread 0
+//               also issues a bulk L2 prefetch of the phase tile sixteen stages
+//               ahead), evaluate sincos on the SFU, split to FP16 hi/lo and
+//               store the A operand in the no-swizzle K-major UMMA layout into
+//               a 6-deep ring (5 for 32-coil groups);
 //   B loader    one bulk copy per stage of the pre-split coil data into a
 //               4-deep ring that the MMA thread releases;
 //   MMA warp    one thread issues tcgen05.mma (kind::f16, M 128, K 16),
-//               commits stage completion to the operand ring's mbarriers and
+//               commits stage completion to the operand rings' mbarriers and
 //               chunk completion to its own, and after seeing a chunk complete
 //               hands its accumulation set to the epilogue; the warp owns the
 //               TMEM allocation (all 512 columns);
@@ -40,6 +41,9 @@
 //               (each its 32-lane quarter) read the finished set with
 //               tcgen05.ld and add it to FP32 register totals, which they store
 //               as the item's partial sums at its end.
+// The A ring is as deep as shared memory allows because the tensor pipe idles
+// whenever the producers cannot refill a slot while the MMAs of the others
+// run; the phase table needs no shared-memory staging of its own.
 // Generic stores into an A slot that MMAs read through the async proxy follow
 // a fence.proxy.async after the slot's release; without it, adjoint rows came
 // out wrong on a GB300.
@@ -54,8 +58,6 @@
 #include <algorithm>
 #include <cmath>
 
-#include <cuda.h>
-#include <cudaTypedefs.h>
 #include <cuda_fp16.h>
 
 #include "nufft.cuh"
@@ -67,43 +69,57 @@ namespace umma {
 
 constexpr int BM = 128;                      // output rows per work item (TMEM lanes)
 constexpr int KS = 32;                       // inputs per pipeline stage
-constexpr int SA = 2;                        // A operand ring depth
 constexpr int SB = 4;                        // B operand ring depth
 constexpr int PS = 2;                        // stages per TMEM accumulation set (64 inputs)
-constexpr int PF = 12;                       // L2 prefetch distance of the phase tiles, in stages
-constexpr int TURN_BYTES = BM * KS * 4;      // 16 KB
-constexpr int A_SUB_BYTES = BM * KS * 2;     // 8 KB per sub-tile (cos hi, cos lo, sin hi, sin lo)
-constexpr int A_BYTES = 4 * A_SUB_BYTES;
+constexpr int PF = 16;                       // L2 prefetch distance of the phase tiles, in stages
+constexpr int MAX_SA = 6;
+constexpr int QUARTER_BYTES = BM * KS * 4;   // one stage's phases: a quarter of a 128 x 128 block (16 KB)
+static_assert(BM == 4 * KS, "a phase block holds four stages along the input dimension");
+constexpr int LA = 2;                        // stages of phases each producer thread keeps in flight
+// Operands in the 128-byte-swizzled K-major layout: rows of 128 bytes, 16-byte chunk c of row r at
+// chunk position c ^ (r & 7), 8-row groups 1 KB apart.  An A stage is two 128-row regions, the
+// cos region holding [hi (32 inputs, 64 B) | lo (64 B)] per row and the sin region the same; a B
+// stage is 2 N0 rows (hi rows, then lo rows) of [cos part (64 B) | sin part (64 B)].  The MMAs
+// step through the 16-input halves by advancing the descriptor start 32 bytes within the row.
+constexpr int A_REGION = BM * 128;           // 16 KB: the cos region, then the sin region
+constexpr int A_BYTES = 2 * A_REGION;
 constexpr int TMEM_COLS = 512;
 constexpr int MAX_SETS = 16;
-constexpr float LO_SCALE = 2048.f;
+constexpr float HI_SCALE = 2048.f;           // A: fixed-point high parts in units of 2^-11
+constexpr float LO_SCALE = 2048.f;           // B: low parts scaled by 2^11
 constexpr float ROUND_MAGIC = 12582912.f;    // 1.5 * 2^23: x + m - m rounds |x| < 2^22 to an integer
-constexpr uint32_t WAIT_POLLS = 1u << 22;
+// mbarrier waits: each try_wait may suspend the thread for up to SUSPEND_NS (it resumes as soon as
+// the phase completes), so that waiting warps take no issue slots from the producers; at most
+// WAIT_POLLS polls (about a second) before a wait counts as timed out
+constexpr uint32_t SUSPEND_NS = 500;
+constexpr uint32_t WAIT_POLLS = 1u << 21;
 
-// warps 0 .. NPW-1 producers, NPW the TMA warp (phase tiles), NPW+1 the MMA warp, NPW+2 the B loader,
-// NPW+3 .. NPW+6 the epilogue
+// warps 0 .. NPW-1 producers, NPW the MMA warp, NPW+1 the B loader, NPW+2 .. NPW+5 the epilogue
 __host__ __device__ constexpr int nprod_warps(int N0) { return N0 <= 32 ? 16 : 8; }
-__host__ __device__ constexpr int nthreads(int N0) { return (nprod_warps(N0) + 7) * 32; }
-// phase-tile ring depth: as many 16 KB tiles in flight as shared memory leaves (HBM latency x
-// bandwidth per SM is about 90 KB)
-__host__ __device__ constexpr int n_turn_stages(int N0) { return N0 <= 32 ? 8 : 6; }
-// B operand of one stage: a cos and a sin sub-tile, each [KS / 8][2 N0 rows: hi then lo][8] halves
-__host__ __device__ constexpr int b_sub_bytes(int N0) { return 2 * N0 * KS * 2; }
-__host__ __device__ constexpr int b_bytes(int N0) { return 2 * b_sub_bytes(N0); }
+__host__ __device__ constexpr int nthreads(int N0) { return (nprod_warps(N0) + 6) * 32; }
+// A operand ring depth: as many 32 KB stages as shared memory leaves beside the B ring, so that
+// the producers run several stages ahead of the tensor pipe
+__host__ __device__ constexpr int n_a_stages(int N0) { return N0 <= 32 ? 6 : 4; }   // even: whole chunks
+// B operand of one stage: 2 N0 rows of 128 bytes
+__host__ __device__ constexpr int b_bytes(int N0) { return 2 * N0 * 128; }
 // TMEM accumulation sets: SET_W(N0) columns each, main at 0, corr1 at N0, corr2 at 2 N0
 __host__ __device__ constexpr int set_w(int N0) { return 4 * N0; }
 __host__ __device__ constexpr int nsets(int N0) {
     return TMEM_COLS / set_w(N0) < MAX_SETS ? TMEM_COLS / set_w(N0) : MAX_SETS;
 }
 
-// offsets in the 1024-aligned dynamic shared memory: phase tiles, A stages, B stages, barriers
-__host__ __device__ constexpr int off_a(int N0) { return n_turn_stages(N0) * TURN_BYTES; }
-__host__ __device__ constexpr int off_b(int N0) { return off_a(N0) + SA * A_BYTES; }
+// offsets in the 1024-aligned dynamic shared memory: A stages from 0, then B stages, then barriers
+__host__ __device__ constexpr int off_b(int N0) { return n_a_stages(N0) * A_BYTES; }
 __host__ __device__ constexpr int bar_off(int N0) { return off_b(N0) + SB * b_bytes(N0); }
-// barriers: tfull[ST] tempty[ST] afull[SA] aempty[SA] bfull[SB] bempty[SB] setfull[MAX_SETS]
-// setempty[MAX_SETS] drain chunk[2], then the TMEM address slot
-constexpr int MAX_ST = 8;
-__host__ __device__ constexpr int nbars() { return 2 * MAX_ST + 2 * SA + 2 * SB + 2 * MAX_SETS + 3; }
+// barriers: cfull[4] (of MAX_SA) bfull[SB] setfull[MAX_SETS] setempty[MAX_SETS] drain chunk[4], then
+// the TMEM address slot.  Per chunk (two stages) the MMA thread waits once (cfull: both stages' A and
+// B in place) and commits twice: chunk[c & 3] frees the chunk's A and B slots, setfull its
+// accumulation set for the epilogue.  (Each mbarrier wait or tcgen05 fence costs the single issuing
+// thread a few hundred cycles of latency, so they are kept to one per 16 MMAs.)
+__host__ __device__ constexpr int nbars() { return MAX_SA + SB + 2 * MAX_SETS + 5; }
+static_assert(bar_off(16) + nbars() * 8 + 16 + 1024 <= 232448, "shared memory (16 columns)");
+static_assert(bar_off(32) + nbars() * 8 + 16 + 1024 <= 232448, "shared memory (32 columns)");
+static_assert(bar_off(64) + nbars() * 8 + 16 + 1024 <= 232448, "shared memory (64 columns)");
 __host__ __device__ constexpr int smem_bytes(int N0) { return bar_off(N0) + nbars() * 8 + 16 + 1024; }
 
 __device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
@@ -126,24 +142,38 @@ __device__ __forceinline__ bool bar_wait(uint32_t bar, uint32_t parity, volatile
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
-            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+            "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
             "selp.u32 %0, 1, 0, p;\n\t}\n"
             : "=r"(done)
-            : "r"(bar), "r"(parity)
+            : "r"(bar), "r"(parity), "n"(SUSPEND_NS)
             : "memory");
         if (done) return true;
-        if (!drain && (it & 1023u) == 1023u && *abort_flag) return false;
+        if (!drain && (it & 63u) == 63u && *abort_flag) return false;
     }
     *abort_flag = 1;
     atomicExch(err, 1);
     return false;
 }
+// Non-blocking test of a phase's completion (no suspension): several can be issued back to back
+// so that their latencies overlap.
+__device__ __forceinline__ uint32_t bar_test(uint32_t bar, uint32_t parity) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return done;
+}
 
-// Shared-memory matrix descriptor: no swizzle, K-major; lbo = byte distance of
-// the core matrices adjacent along K, sbo = of those adjacent along M / N.
-__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
-    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
-           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | ((uint64_t)1 << 46);
+// Shared-memory matrix descriptor, K-major with 128-byte swizzle: start address >> 4 in bits 0-13,
+// the leading offset (unused by this layout; 16 bytes) in bits 16-29, the 8-row group stride (1 KB)
+// >> 4 in bits 32-45, descriptor version 1 at bit 46, layout type 2 (128-byte swizzle) in bits 61-63.
+__device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
+    return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+           ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
 }
 // Instruction descriptor, kind::f16: D F32 (bits 4-5 = 1), A and B F16, both K-major,
 // N >> 3 at bit 17, M >> 4 at bit 24.
@@ -156,6 +186,17 @@ __device__ __forceinline__ void mma(uint32_t d, uint64_t a, uint64_t b, uint32_t
         "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
         "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d),
         "l"(a), "l"(b), "r"(id), "r"(acc));
+}
+// The same with each descriptor given as its two 32-bit words: the start address (bits 0-13 of the
+// low word, byte address >> 4) of a descriptor advances by a plain 32-bit add, which cannot carry
+// into the offset field above it because shared-memory addresses stay below 2^18.
+__device__ __forceinline__ void mma2(uint32_t d, uint32_t alo, uint32_t ahi, uint32_t blo, uint32_t bhi, uint32_t id,
+                                     uint32_t acc) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t.reg .b64 da, db;\n\t"
+        "mov.b64 da, {%1, %2};\n\tmov.b64 db, {%3, %4};\n\tsetp.ne.b32 p, %6, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], da, db, %5, p;\n\t}\n" ::"r"(d),
+        "r"(alo), "r"(ahi), "r"(blo), "r"(bhi), "r"(id), "r"(acc));
 }
 __device__ __forceinline__ void commit(uint32_t bar) {
     asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
@@ -201,45 +242,66 @@ __device__ __forceinline__ void tmem_ld16(uint32_t ta, float (&a)[16]) {
 
 __device__ __forceinline__ uint32_t h2bits(__half2 h) { return *reinterpret_cast<uint32_t*>(&h); }
 
-// Work item w -> row tile and the stage range of its K split (balanced integer split).
-__device__ __forceinline__ void item_range(long long w, int nsplit, long long Q, long long& rt, long long& sp,
-                                           long long& qa, long long& qb) {
+// Work item w -> row tile and the stage range of its K split: a balanced integer split of the
+// phase blocks (four stages each), so that an item reads whole 64 KB blocks.
+__host__ __device__ __forceinline__ void item_range(long long w, int nsplit, long long Q, long long& rt,
+                                                    long long& sp, long long& qa, long long& qb) {
+    const long long Qb = (Q + 3) >> 2;
     rt = w / nsplit;
     sp = w - rt * nsplit;
-    qa = sp * Q / nsplit;
-    qb = (sp + 1) * Q / nsplit;
+    qa = std::min(Q, 4 * (sp * Qb / nsplit));
+    qb = std::min(Q, 4 * ((sp + 1) * Qb / nsplit));
 }
+
+// Walks a CTA's stages in order: items blockIdx.x, + gridDim.x, ..., each from qa to qb - 1.
+struct Cursor {
+    int w, rt, q, qb;
+    bool valid;
+    __device__ __forceinline__ void enter(long long nitems, int nsplit, long long Q) {
+        valid = w < nitems;
+        if (valid) {
+            long long rt_, sp_, qa_, qb_;
+            item_range(w, nsplit, Q, rt_, sp_, qa_, qb_);
+            rt = (int)rt_;
+            q = (int)qa_;
+            qb = (int)qb_;
+        }
+    }
+    __device__ __forceinline__ void next(long long nitems, int nsplit, long long Q) {
+        if (++q >= qb) {
+            w += gridDim.x;
+            enter(nitems, nsplit, Q);
+        }
+    }
+};
 
 }  // namespace umma
 
-// partial[sp][row][N0] for every work item.  `turn_map` tiles the [V][M] phase table: forward
-// box {128 samples, 32 voxels} (no swizzle), adjoint box {32 samples, 128 voxels} (128-byte
-// swizzle).  bglob: the B operand in per-stage blocks laid out as in shared memory.
+// partial[sp][row][N0] for every work item.  tblk: the phase table in radians in 128 x 128 blocks
+// ([V / 128][M / 128][128 voxels][128 samples], zero-padded; mblk blocks along M).  bglob: the B
+// operand in per-stage blocks laid out as in shared memory.
 template <bool ADJ, int N0>
 __global__ void __launch_bounds__(umma::nthreads(N0), 1)
-    sho_umma_kernel(const __grid_constant__ CUtensorMap turn_map, const __half* __restrict__ bglob,
-                    float* __restrict__ partial, long long R, long long Q, int nsplit, long long nitems, int* err,
-                    const int* active) {
+    sho_umma_kernel(const float* __restrict__ tblk, long long V, long long M, long long mblk,
+                    const __half* __restrict__ bglob, float* __restrict__ partial, long long Q, int nsplit,
+                    long long nitems, int* err, const int* active) {
     using namespace umma;
     constexpr int NS = nsets(N0);
     constexpr int SW = set_w(N0);
     constexpr int NPW = nprod_warps(N0), NPROD = NPW * 32;
-    constexpr int WARP_TMA = NPW, WARP_MMA = NPW + 1, WARP_B = NPW + 2;
-    constexpr int ST = n_turn_stages(N0);
-    constexpr int OFF_A = off_a(N0), OFF_B = off_b(N0);
+    constexpr int WARP_MMA = NPW, WARP_B = NPW + 1;
+    constexpr int SA = n_a_stages(N0);
+    constexpr int OFF_A = 0, OFF_B = off_b(N0);
+    const long long R = ADJ ? V : M;
     constexpr int CPT = (BM * KS / 8) / NPROD;     // 8-input chunks per producer thread and stage
     if (active && *active) return;
     extern __shared__ uint8_t smem_raw[];
     uint8_t* sm = smem_raw + ((1024u - (su32(smem_raw) & 1023u)) & 1023u);
     const uint32_t s0 = su32(sm);
     const uint32_t bars = s0 + bar_off(N0);
-    auto tfull = [&](int i) { return bars + 8u * i; };
-    auto tempty = [&](int i) { return bars + 8u * (MAX_ST + i); };
-    auto afull = [&](int i) { return bars + 8u * (2 * MAX_ST + i); };
-    auto aempty = [&](int i) { return bars + 8u * (2 * MAX_ST + SA + i); };
-    auto bfull = [&](int i) { return bars + 8u * (2 * MAX_ST + 2 * SA + i); };
-    auto bempty = [&](int i) { return bars + 8u * (2 * MAX_ST + 2 * SA + SB + i); };
-    constexpr int SET0 = 2 * MAX_ST + 2 * SA + 2 * SB;
+    auto cfull = [&](int i) { return bars + 8u * i; };     // chunk c's operands ready: cfull[c & 3]
+    auto bfull = [&](int i) { return bars + 8u * (MAX_SA + i); };
+    constexpr int SET0 = MAX_SA + SB;
     auto setfull = [&](int i) { return bars + 8u * (SET0 + i); };
     auto setempty = [&](int i) { return bars + 8u * (SET0 + MAX_SETS + i); };
     const uint32_t drain = bars + 8u * (SET0 + 2 * MAX_SETS);
@@ -250,25 +312,15 @@ __global__ void __launch_bounds__(umma::nthreads(N0), 1)
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if (tid == 0) {
         abort_flag = 0;
-        for (int i = 0; i < ST; ++i) {
-            bar_init(tfull(i), 1);
-            bar_init(tempty(i), NPROD);
-        }
-        for (int i = 0; i < SA; ++i) {
-            bar_init(afull(i), NPROD);
-            bar_init(aempty(i), 1);
-        }
-        for (int i = 0; i < SB; ++i) {
-            bar_init(bfull(i), 1);
-            bar_init(bempty(i), 1);
-        }
+        // per chunk: one arrival per producer warp
+        for (int i = 0; i < 4; ++i) bar_init(cfull(i), NPW);
+        for (int i = 0; i < SB / 2; ++i) bar_init(bfull(i), 1);   // per B chunk slot (two stages)
         for (int i = 0; i < NS; ++i) {
             bar_init(setfull(i), 1);
-            bar_init(setempty(i), 128);
+            bar_init(setempty(i), 4);          // one arrival per epilogue warp
         }
         bar_init(drain, 1);
-        bar_init(chunkbar(0), 1);
-        bar_init(chunkbar(1), 1);
+        for (int i = 0; i < 4; ++i) bar_init(chunkbar(i), 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     if (warp == WARP_MMA) {
@@ -284,159 +336,178 @@ __global__ void __launch_bounds__(umma::nthreads(N0), 1)
     if (warp < NPW) {
         // ------------------------------------------------------------ producers --
         // A = cos / sin of the phase, each split into a high part hi = round(2^11 v) (an integer of at
-        // most 2048, exact in FP16) and a low part lo = 2^11 (2^11 v - hi) (|lo| <= 1024): the MMAs
-        // then give 2^11 main and 2^22 corr, which the reduce kernel scales back
-        const int r = tid & (BM - 1);
-        const int kq = tid >> 7;          // chunks kq + j NPROD / 128 of each stage (8 inputs each)
-        long long g = 0;
-        for (long long w = blockIdx.x; w < nitems && !abort_flag; w += gridDim.x) {
+        // most 2048, exact in FP16) and a low part lo = 2^11 v - hi (|lo| <= 1/2): the MMAs then give
+        // 2^11 times the sums, which the reduce kernel scales back.  Each thread loads
+        // its phases of the next stage into registers while it works on this one; thread 0 keeps the
+        // L2 prefetches PF stages ahead of those loads.
+        // (row, 8-input chunk) pairs of a stage: 128 x 4, CPT per thread.  Forward: lanes run along
+        // the rows (samples, contiguous in the table); adjoint: four lanes share a row (a voxel's 32
+        // samples, 128 contiguous bytes), so that a warp's loads touch 8 lines instead of 32.
+        auto row_of = [&](int j) { return ADJ ? (tid + j * NPROD) >> 2 : tid & (BM - 1); };
+        auto chunk_of = [&](int j) { return ADJ ? (tid + j * NPROD) & 3 : (tid >> 7) + j * (NPROD / BM); };
+        // out-of-range phases read as 0: their B rows are zero, or their output rows are dropped
+        // stage q of row tile rt: block (q / 4, rt) forward, (rt, q / 4) adjoint, inputs 32 (q % 4) ..
+        auto stage_block = [&](const Cursor& cs) {
+            const long long qb4 = cs.q >> 2;
+            return tblk + (ADJ ? (long long)cs.rt * mblk + qb4 : qb4 * mblk + cs.rt) * (BM * BM);
+        };
+        auto load_stage = [&](const Cursor& cs, float (&t)[CPT][8]) {
+            const float* blk = stage_block(cs);
+            const int sub = (cs.q & 3) * KS;
+#pragma unroll
+            for (int j = 0; j < CPT; ++j) {
+                const int r = row_of(j), kc = chunk_of(j);
+                if (ADJ) {
+                    // row r = voxel: 8 consecutive samples, 32 bytes
+                    const float4* p = reinterpret_cast<const float4*>(blk + r * BM + sub + kc * 8);
+                    const float4 lo4 = __ldcs(p), hi4 = __ldcs(p + 1);
+                    t[j][0] = lo4.x; t[j][1] = lo4.y; t[j][2] = lo4.z; t[j][3] = lo4.w;
+                    t[j][4] = hi4.x; t[j][5] = hi4.y; t[j][6] = hi4.z; t[j][7] = hi4.w;
+                } else {
+                    // row r = sample, 8 voxels: each warp load is 128 consecutive bytes of one voxel row
+                    const float* p = blk + (sub + kc * 8) * BM + r;
+#pragma unroll
+                    for (int e = 0; e < 8; ++e) t[j][e] = __ldcs(p + e * BM);
+                }
+            }
+        };
+        // this CTA's stage count
+        long long nst = 0;
+        for (long long w = blockIdx.x; w < nitems; w += gridDim.x) {
             long long rt, sp, qa, qb;
             item_range(w, nsplit, Q, rt, sp, qa, qb);
-            for (long long q = qa; q < qb; ++q, ++g) {
-                const int ts = (int)(g % ST), as = (int)(g % SA);
-                if (!bar_wait(tfull(ts), (uint32_t)((g / ST) & 1), &abort_flag, err)) break;
-                if (g >= SA && !bar_wait(aempty(as), (uint32_t)(((g / SA) + 1) & 1), &abort_flag, err)) break;
-                // the MMAs of this slot's previous use read it through the async proxy: order them
-                // before this thread's generic stores to it
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                const float* tile = reinterpret_cast<const float*>(sm + ts * TURN_BYTES);
-                float t[CPT][8];
+            nst += qb - qa;
+        }
+        Cursor ld, pre;       // the next stage to load, the next stage to prefetch into L2
+        ld.w = blockIdx.x;
+        ld.enter(nitems, nsplit, Q);
+        pre = ld;
+        // one 16 KB quarter of a block per stage: over a block's four stages the whole block is
+        // fetched, PF stages before it is read
+        auto prefetch = [&]() {
+            const float* q4 = stage_block(pre) + (pre.q & 3) * (BM * KS);
+            asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(q4), "n"(QUARTER_BYTES) : "memory");
+            pre.next(nitems, nsplit, Q);
+        };
+        if (tid == 0)
+            for (int k = 0; k < PF && pre.valid; ++k) prefetch();
+        // register ring: while stage g is split and stored, stages g + 1 .. g + LA are in flight
+        float tr[LA + 1][CPT][8];
+        int as = 0;            // A slot of stage g
 #pragma unroll
-                for (int j = 0; j < CPT; ++j) {
-                    const int kc = kq + j * (NPROD / BM);
-                    if (ADJ) {
-                        // [128 voxels][32 samples], 128-byte swizzle: 16-byte chunk c of row r at c ^ (r & 7)
-                        const float4 lo4 = *reinterpret_cast<const float4*>(
-                            reinterpret_cast<const uint8_t*>(tile) + r * 128 + (((2 * kc) ^ (r & 7)) << 4));
-                        const float4 hi4 = *reinterpret_cast<const float4*>(
-                            reinterpret_cast<const uint8_t*>(tile) + r * 128 + (((2 * kc + 1) ^ (r & 7)) << 4));
-                        t[j][0] = lo4.x; t[j][1] = lo4.y; t[j][2] = lo4.z; t[j][3] = lo4.w;
-                        t[j][4] = hi4.x; t[j][5] = hi4.y; t[j][6] = hi4.z; t[j][7] = hi4.w;
-                    } else {
-                        // [32 voxels][128 samples]
+        for (int u = 0; u < LA; ++u)
+            if (ld.valid) {
+                load_stage(ld, tr[u]);
+                ld.next(nitems, nsplit, Q);
+            }
+        for (long long g0 = 0; g0 < nst && !abort_flag; g0 += LA + 1) {
 #pragma unroll
-                        for (int e = 0; e < 8; ++e) t[j][e] = tile[(kc * 8 + e) * BM + r];
-                    }
+            for (int slot = 0; slot < LA + 1; ++slot) {
+                const long long g = g0 + slot;
+                if (g >= nst) break;
+                if (ld.valid) {
+                    load_stage(ld, tr[(slot + LA) % (LA + 1)]);
+                    ld.next(nitems, nsplit, Q);
                 }
-                bar_arrive(tempty(ts));
-                uint8_t* a = sm + OFF_A + as * A_BYTES;
+                if (tid == 0 && pre.valid) prefetch();
+                float (&t)[CPT][8] = tr[slot];
+                // cos hi, cos lo, sin hi, sin lo of this thread's 8-input chunks, as FP16 pairs
+                uint32_t pk[CPT][4][4];
 #pragma unroll
                 for (int j = 0; j < CPT; ++j) {
-                    const int kc = kq + j * (NPROD / BM);
-                    uint32_t chi[4], clo[4], shi[4], slo[4];
 #pragma unroll
                     for (int e = 0; e < 4; ++e) {
                         float chv[2], shv[2], clv[2], slv[2];
 #pragma unroll
                         for (int u = 0; u < 2; ++u) {
                             float sv, cv;
-                            __sincosf(6.28318530717958647692f * t[j][2 * e + u], &sv, &cv);
-                            const float cs = __fmul_rn(cv, LO_SCALE), ss = __fmul_rn(sv, LO_SCALE);
-                            chv[u] = __fsub_rn(__fadd_rn(cs, ROUND_MAGIC), ROUND_MAGIC);
-                            shv[u] = __fsub_rn(__fadd_rn(ss, ROUND_MAGIC), ROUND_MAGIC);
-                            clv[u] = __fmul_rn(__fsub_rn(cs, chv[u]), LO_SCALE);
-                            slv[u] = __fmul_rn(__fsub_rn(ss, shv[u]), LO_SCALE);
+                            __sincosf(t[j][2 * e + u], &sv, &cv);
+                            // hi = round(2^11 v) in one rounding of the exact 2^11 v + 1.5 2^23; the
+                            // residual 2^11 v - hi is exact in one FMA
+                            chv[u] = __fsub_rn(__fmaf_rn(cv, HI_SCALE, ROUND_MAGIC), ROUND_MAGIC);
+                            shv[u] = __fsub_rn(__fmaf_rn(sv, HI_SCALE, ROUND_MAGIC), ROUND_MAGIC);
+                            clv[u] = __fmaf_rn(cv, HI_SCALE, -chv[u]);
+                            slv[u] = __fmaf_rn(sv, HI_SCALE, -shv[u]);
                         }
-                        chi[e] = h2bits(__floats2half2_rn(chv[0], chv[1]));
-                        shi[e] = h2bits(__floats2half2_rn(shv[0], shv[1]));
-                        clo[e] = h2bits(__floats2half2_rn(clv[0], clv[1]));
-                        slo[e] = h2bits(__floats2half2_rn(slv[0], slv[1]));
+                        pk[j][0][e] = h2bits(__floats2half2_rn(chv[0], chv[1]));
+                        pk[j][1][e] = h2bits(__floats2half2_rn(clv[0], clv[1]));
+                        pk[j][2][e] = h2bits(__floats2half2_rn(shv[0], shv[1]));
+                        pk[j][3][e] = h2bits(__floats2half2_rn(slv[0], slv[1]));
                     }
-                    const int off = kc * (BM * 16) + r * 16;   // core matrices: 8 rows x 16 B, rows 16 B apart
-                    *reinterpret_cast<uint4*>(a + 0 * A_SUB_BYTES + off) = make_uint4(chi[0], chi[1], chi[2], chi[3]);
-                    *reinterpret_cast<uint4*>(a + 1 * A_SUB_BYTES + off) = make_uint4(clo[0], clo[1], clo[2], clo[3]);
-                    *reinterpret_cast<uint4*>(a + 2 * A_SUB_BYTES + off) = make_uint4(shi[0], shi[1], shi[2], shi[3]);
-                    *reinterpret_cast<uint4*>(a + 3 * A_SUB_BYTES + off) = make_uint4(slo[0], slo[1], slo[2], slo[3]);
                 }
-                asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-                bar_arrive(afull(as));
+                // Once per chunk (two stages), at its first stage: the previous chunk's stores, issued
+                // before this stage's sincos, have drained by now: order them before the async
+                // proxy's reads and hand that chunk to the MMA thread; then wait until the chunk that
+                // last used this chunk's two A slots (SA is even) has completed.  Lane 0 waits, the
+                // warp follows it (one poller per warp on the barrier).
+                if ((g & 1) == 0) {
+                    if (g > 0) {
+                        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                        __syncwarp();
+                        if (lane == 0) bar_arrive(cfull((int)(((g >> 1) - 1) & 3)));
+                    }
+                    if (g >= SA) {
+                        const long long k = (g - SA) >> 1;
+                        int okw = 1;
+                        if (lane == 0)
+                            okw = bar_wait(chunkbar((int)(k & 3)), (uint32_t)((k >> 2) & 1), &abort_flag, err);
+                        __syncwarp();
+                        if (!__shfl_sync(0xffffffffu, okw, 0)) break;
+                    }
+                }
+                uint8_t* a = sm + OFF_A + as * A_BYTES;
+#pragma unroll
+                for (int j = 0; j < CPT; ++j) {
+                    const int r = row_of(j), kc = chunk_of(j);
+                    // row r of each region; hi in chunk kc, lo in chunk 4 + kc, swizzled by r & 7
+                    uint8_t* rc = a + r * 128;
+                    uint8_t* rs = rc + A_REGION;
+                    const int sw = r & 7;
+                    *reinterpret_cast<uint4*>(rc + ((kc ^ sw) << 4)) = make_uint4(pk[j][0][0], pk[j][0][1], pk[j][0][2], pk[j][0][3]);
+                    *reinterpret_cast<uint4*>(rc + (((4 + kc) ^ sw) << 4)) = make_uint4(pk[j][1][0], pk[j][1][1], pk[j][1][2], pk[j][1][3]);
+                    *reinterpret_cast<uint4*>(rs + ((kc ^ sw) << 4)) = make_uint4(pk[j][2][0], pk[j][2][1], pk[j][2][2], pk[j][2][3]);
+                    *reinterpret_cast<uint4*>(rs + (((4 + kc) ^ sw) << 4)) = make_uint4(pk[j][3][0], pk[j][3][1], pk[j][3][2], pk[j][3][3]);
+                }
+                if (++as == SA) as = 0;
             }
+        }
+        // the last chunk's hand-off
+        if (nst > 0 && !abort_flag) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncwarp();
+            if (lane == 0) bar_arrive(cfull((int)(((nst - 1) >> 1) & 3)));
         }
     } else if (warp == WARP_B) {
         // -------------------------------------------------------------- B loader --
-        // the stage's B operand (coil data, FP16 hi / lo, both parts) by one bulk copy into a ring
-        // that the MMA thread releases stage by stage
-        long long g = 0;
+        // a chunk's B operand (coil data, FP16 hi / lo, both parts, two stages: adjacent in global
+        // and in shared memory) by one bulk copy into a ring of SB / 2 chunk slots, completing on the
+        // slot's bfull; slot reuse waits for the completion of the chunk that last read it
+        constexpr int NBC = SB / 2;
+        long long c = 0;   // chunk copies issued
         if (lane == 0) {
-            for (long long w = blockIdx.x; w < nitems && !abort_flag; w += gridDim.x) {
+            bool ok = true;
+            for (long long w = blockIdx.x; w < nitems && ok && !abort_flag; w += gridDim.x) {
                 long long rt, sp, qa, qb;
                 item_range(w, nsplit, Q, rt, sp, qa, qb);
-                bool ok = true;
-                for (long long q = qa; q < qb; ++q, ++g) {
-                    const int bs = (int)(g % SB);
-                    if (g >= SB && !bar_wait(bempty(bs), (uint32_t)(((g / SB) + 1) & 1), &abort_flag, err)) {
+                for (long long q = qa; q < qb; q += PS) {
+                    const int bc = (int)(c % NBC);
+                    const long long k = c - NBC;
+                    if (c >= NBC && !bar_wait(chunkbar((int)(k & 3)), (uint32_t)((k >> 2) & 1), &abort_flag, err)) {
                         ok = false;
                         break;
                     }
-                    bar_expect(bfull(bs), (uint32_t)b_bytes(N0));
+                    bar_expect(bfull(bc), (uint32_t)(PS * b_bytes(N0)));
                     asm volatile(
                         "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                            s0 + OFF_B + bs * b_bytes(N0)),
-                        "l"(bglob + (size_t)q * (b_bytes(N0) / 2)), "r"((uint32_t)b_bytes(N0)), "r"(bfull(bs))
+                            s0 + OFF_B + bc * (PS * b_bytes(N0))),
+                        "l"(bglob + (size_t)q * (b_bytes(N0) / 2)), "r"((uint32_t)(PS * b_bytes(N0))), "r"(bfull(bc))
                         : "memory");
+                    ++c;
                 }
-                if (!ok) break;
             }
             if (abort_flag) {   // the copies in flight land before the CTA exits
-                for (long long k = std::max<long long>(0, g - SB); k < g; ++k)
-                    bar_wait(bfull((int)(k % SB)), (uint32_t)((k / SB) & 1), &abort_flag, err, true);
-            }
-        }
-        __syncwarp();
-    } else if (warp == WARP_TMA) {
-        // ------------------------------------------------------------------ TMA --
-        // Each phase tile is also prefetched into L2 PF stages before its load, so that the
-        // ring's loads see L2 rather than HBM latency.
-        long long g = 0;
-        if (lane == 0) {
-            long long w2 = blockIdx.x, rt2 = 0, sp2 = 0, qa2 = 0, qb2 = 0, q2 = 0;
-            bool la = w2 < nitems;
-            if (la) {
-                item_range(w2, nsplit, Q, rt2, sp2, qa2, qb2);
-                q2 = qa2;
-            }
-            auto prefetch_next = [&]() {
-                if (!la) return;
-                const int px = ADJ ? (int)(q2 * KS) : (int)(rt2 * BM);
-                const int py = ADJ ? (int)(rt2 * BM) : (int)(q2 * KS);
-                asm volatile("cp.async.bulk.prefetch.tensor.2d.L2.global.tile [%0, {%1, %2}];" ::"l"(&turn_map),
-                             "r"(px), "r"(py)
-                             : "memory");
-                if (++q2 >= qb2) {
-                    w2 += gridDim.x;
-                    la = w2 < nitems;
-                    if (la) {
-                        item_range(w2, nsplit, Q, rt2, sp2, qa2, qb2);
-                        q2 = qa2;
-                    }
-                }
-            };
-            for (int k = 0; k < PF; ++k) prefetch_next();
-            for (long long w = blockIdx.x; w < nitems && !abort_flag; w += gridDim.x) {
-                long long rt, sp, qa, qb;
-                item_range(w, nsplit, Q, rt, sp, qa, qb);
-                bool ok = true;
-                for (long long q = qa; q < qb; ++q, ++g) {
-                    const int ts = (int)(g % ST);
-                    if (g >= ST && !bar_wait(tempty(ts), (uint32_t)(((g / ST) + 1) & 1), &abort_flag, err)) {
-                        ok = false;
-                        break;
-                    }
-                    bar_expect(tfull(ts), (uint32_t)TURN_BYTES);
-                    const int cx = ADJ ? (int)(q * KS) : (int)(rt * BM);    // samples (inner dimension)
-                    const int cy = ADJ ? (int)(rt * BM) : (int)(q * KS);    // voxels
-                    asm volatile(
-                        "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, "
-                        "{%2, %3}], [%4];" ::"r"(s0 + ts * TURN_BYTES),
-                        "l"(&turn_map), "r"(cx), "r"(cy), "r"(tfull(ts))
-                        : "memory");
-                    prefetch_next();
-                }
-                if (!ok) break;
-            }
-            if (abort_flag) {   // let the phase tiles in flight land
-                for (long long k = std::max<long long>(0, g - ST); k < g; ++k)
-                    bar_wait(tfull((int)(k % ST)), (uint32_t)((k / ST) & 1), &abort_flag, err, true);
+                for (long long k = std::max<long long>(0, c - NBC); k < c; ++k)
+                    bar_wait(bfull((int)(k % NBC)), (uint32_t)((k / NBC) & 1), &abort_flag, err, true);
             }
         }
         __syncwarp();
@@ -444,74 +515,56 @@ __global__ void __launch_bounds__(umma::nthreads(N0), 1)
         // ------------------------------------------------------------------ MMA --
         if (lane == 0) {
             constexpr uint32_t ID2 = idesc(BM, 2 * N0), ID1 = idesc(BM, N0);
-            constexpr uint32_t LBO_A = BM * 16, LBO_B = 2 * N0 * 16;   // K-direction core-matrix strides
-            long long g = 0, c = 0;
+            // descriptors of A slot 0 / B slot 0 as 32-bit words
+            const uint64_t da0 = sdesc_sw128(s0 + OFF_A), db0 = sdesc_sw128(s0 + OFF_B);
+            const uint32_t da_lo = (uint32_t)da0, da_hi = (uint32_t)(da0 >> 32);
+            const uint32_t db_lo = (uint32_t)db0, db_hi = (uint32_t)(db0 >> 32);
+            long long c = 0;
+            int as = 0, bs = 0;          // operand slots of the current stage
             bool ok = true;
-            // A set goes to the epilogue only after this thread has seen its MMAs complete: each
-            // chunk's MMAs are committed to chunkbar[c & 1], and once the next chunk's MMAs are
-            // queued this thread waits for that barrier and then arrives on setfull.  (Epilogue
-            // warps waiting directly on a tcgen05.commit arrival read incomplete accumulators.)
-            long long pend = -1;
-            int pend_set = 0;
-            auto release_pending = [&]() {
-                if (pend < 0) return true;
-                if (!bar_wait(chunkbar((int)(pend & 1)), (uint32_t)((pend >> 1) & 1), &abort_flag, err)) return false;
-                fence_before();
-                bar_arrive(setfull(pend_set));
-                pend = -1;
-                return true;
-            };
             for (long long w = blockIdx.x; w < nitems && ok && !abort_flag; w += gridDim.x) {
                 long long rt, sp, qa, qb;
                 item_range(w, nsplit, Q, rt, sp, qa, qb);
-                for (long long q0 = qa; q0 < qb && ok; q0 += PS, ++c) {
+                for (long long q0 = qa; q0 < qb; q0 += PS, ++c) {   // chunks of two stages
                     const int set = (int)(c % NS);
-                    if (c >= NS && !bar_wait(setempty(set), (uint32_t)(((c / NS) + 1) & 1), &abort_flag, err)) {
+                    const uint32_t se = setempty(set), se_ph = (uint32_t)(((c / NS) + 1) & 1);
+                    const uint32_t cf = cfull((int)(c & 3)), cf_ph = (uint32_t)((c >> 2) & 1);
+                    const uint32_t bf = bfull((int)(c % (SB / 2))), bf_ph = (uint32_t)((c / (SB / 2)) & 1);
+                    // the set free, the A stages stored, the B chunk landed: three probes issued back to
+                    // back, a bounded wait only for those not yet complete
+                    const uint32_t t1 = c >= NS ? bar_test(se, se_ph) : 1u;
+                    const uint32_t t2 = bar_test(cf, cf_ph);
+                    const uint32_t t3 = bar_test(bf, bf_ph);
+                    if ((!t1 && !bar_wait(se, se_ph, &abort_flag, err)) || (!t2 && !bar_wait(cf, cf_ph, &abort_flag, err)) ||
+                        (!t3 && !bar_wait(bf, bf_ph, &abort_flag, err))) {
                         ok = false;
                         break;
                     }
                     fence_after();
                     const uint32_t dset = tmem + (uint32_t)(set * SW);
-                    const long long q1 = std::min<long long>(q0 + PS, qb);
-                    for (long long q = q0; q < q1; ++q, ++g) {
-                        const int as = (int)(g % SA), bs = (int)(g % SB);
-                        if (!bar_wait(bfull(bs), (uint32_t)((g / SB) & 1), &abort_flag, err) ||
-                            !bar_wait(afull(as), (uint32_t)((g / SA) & 1), &abort_flag, err)) {
-                            ok = false;
-                            break;
-                        }
-                        fence_after();
-                        const uint32_t a0 = s0 + OFF_A + as * A_BYTES;
-                        const uint32_t b0 = s0 + OFF_B + bs * b_bytes(N0);
+#pragma unroll
+                    for (int h = 0; h < PS; ++h) {
+                        // descriptor low words of this stage's A and B slots; offsets below in 16-byte units
+                        const uint32_t alo = da_lo + (uint32_t)(as * (A_BYTES >> 4));
+                        const uint32_t blo = db_lo + (uint32_t)(bs * (b_bytes(N0) >> 4));
 #pragma unroll
                         for (int j = 0; j < KS / 16; ++j) {
-                            const uint32_t ao = j * 2 * LBO_A, bo = j * 2 * LBO_B;
-                            const uint64_t ach = sdesc(a0 + 0 * A_SUB_BYTES + ao, LBO_A, 128);
-                            const uint64_t acl = sdesc(a0 + 1 * A_SUB_BYTES + ao, LBO_A, 128);
-                            const uint64_t ash = sdesc(a0 + 2 * A_SUB_BYTES + ao, LBO_A, 128);
-                            const uint64_t asl = sdesc(a0 + 3 * A_SUB_BYTES + ao, LBO_A, 128);
-                            const uint64_t bc = sdesc(b0 + bo, LBO_B, 128);
-                            const uint64_t bs = sdesc(b0 + b_sub_bytes(N0) + bo, LBO_B, 128);
-                            const uint32_t acc = (q == q0 && j == 0) ? 0u : 1u;
-                            mma(dset, ach, bc, ID2, acc);            // [main | corr1] += cos_hi x [Bc_hi; Bc_lo]
-                            mma(dset + 2 * N0, acl, bc, ID1, acc);   // corr2 += cos_lo x Bc_hi
-                            mma(dset, ash, bs, ID2, 1u);
-                            mma(dset + 2 * N0, asl, bs, ID1, 1u);
+                            const uint32_t ko = (uint32_t)j * (32 >> 4);   // 16 inputs = 32 bytes along the row
+                            const uint32_t acc = (h == 0 && j == 0) ? 0u : 1u;
+                            constexpr uint32_t LO = 64 >> 4, SIN = A_REGION >> 4;
+                            // [main | corr1] += cos_hi x [Bc_hi; Bc_lo];  corr2 += cos_lo x Bc_hi; then the sin parts
+                            mma2(dset, alo + ko, da_hi, blo + ko, db_hi, ID2, acc);
+                            mma2(dset + 2 * N0, alo + LO + ko, da_hi, blo + ko, db_hi, ID1, acc);
+                            mma2(dset, alo + SIN + ko, da_hi, blo + LO + ko, db_hi, ID2, 1u);
+                            mma2(dset + 2 * N0, alo + SIN + LO + ko, da_hi, blo + LO + ko, db_hi, ID1, 1u);
                         }
-                        commit(aempty(as));
-                        commit(bempty(bs));
+                        if (++as == SA) as = 0;
+                        if (++bs == SB) bs = 0;
                     }
-                    if (!ok) break;
-                    commit(chunkbar((int)(c & 1)));
-                    if (!release_pending()) {
-                        ok = false;
-                        break;
-                    }
-                    pend = c;
-                    pend_set = set;
+                    commit(chunkbar((int)(c & 3)));   // the chunk's A and B slots
+                    commit(setfull(set));              // its accumulation set, for the epilogue
                 }
             }
-            if (ok) release_pending();
             // every MMA this thread issued completes before TMEM is freed
             commit(drain);
             bar_wait(drain, 0u, &abort_flag, err, true);
@@ -532,10 +585,12 @@ __global__ void __launch_bounds__(umma::nthreads(N0), 1)
             for (int k = 0; k < N0; ++k) tot[k] = 0.f;
             for (long long q0 = qa; q0 < qb; q0 += PS, ++c) {
                 const int set = (int)(c % NS);
-                // every lane waits (acquire), then the warp reconverges before the warp-collective
-                // tcgen05.ld; a wait that ran out on any lane stops the whole warp
-                const bool got = bar_wait(setfull(set), (uint32_t)((c / NS) & 1), &abort_flag, err);
-                if (!__all_sync(0xffffffffu, got)) {
+                // lane 0 waits (acquire), the warp reconverges behind it before the warp-collective
+                // tcgen05.ld; a wait that ran out stops the whole warp
+                int got = 1;
+                if (lane == 0) got = bar_wait(setfull(set), (uint32_t)((c / NS) & 1), &abort_flag, err);
+                __syncwarp();
+                if (!__shfl_sync(0xffffffffu, got, 0)) {
                     ok = false;
                     break;
                 }
@@ -544,15 +599,16 @@ __global__ void __launch_bounds__(umma::nthreads(N0), 1)
 #pragma unroll
                 for (int cb = 0; cb < N0; cb += 16) {
                     float mv[16], cv[16];
-                    tmem_ld16x2(ts + N0 + cb, ts + 2 * N0 + cb, mv, cv);     // corr1, corr2
+                    tmem_ld16x2(ts + N0 + cb, ts + 2 * N0 + cb, mv, cv);     // corr1 (B lo x 2^11), corr2
 #pragma unroll
-                    for (int k = 0; k < 16; ++k) cv[k] += mv[k];
+                    for (int k = 0; k < 16; ++k) cv[k] = __fmaf_rn(mv[k], 1.f / LO_SCALE, cv[k]);
                     tmem_ld16(ts + cb, mv);                                  // main
 #pragma unroll
-                    for (int k = 0; k < 16; ++k) tot[cb + k] += mv[k] + cv[k] * (1.f / LO_SCALE);
+                    for (int k = 0; k < 16; ++k) tot[cb + k] += mv[k] + cv[k];
                 }
                 fence_before();
-                bar_arrive(setempty(set));
+                __syncwarp();
+                if (lane == 0) bar_arrive(setempty(set));
             }
             if (!ok) break;
             const long long grow = rt * BM + row;
@@ -572,6 +628,20 @@ __global__ void __launch_bounds__(umma::nthreads(N0), 1)
     }
 }
 
+// The [V][M] phase table (turns) as radians, FP32(2 pi t), in 128 x 128 blocks: block (vb, mb) at
+// (vb mblk + mb) 128^2, voxel-major inside, zero beyond V and M.  One CTA per block.
+__global__ void sho_umma_block_kernel(const float* __restrict__ turn, long long V, long long M, long long mblk,
+                                      float* __restrict__ tblk) {
+    using namespace umma;
+    const long long blk = blockIdx.x;
+    const long long vb = blk / mblk, mb = blk - vb * mblk;
+    float* dst = tblk + blk * (BM * BM);
+    for (int i = threadIdx.x; i < BM * BM; i += blockDim.x) {
+        const long long v = vb * BM + (i >> 7), m = mb * BM + (i & (BM - 1));
+        dst[i] = (v < V && m < M) ? __fmul_rn(6.28318530717958647692f, turn[v * M + m]) : 0.f;
+    }
+}
+
 // Per-column max |re|, |im| of in[L, nb] as float bits (cmax zeroed by the caller).
 __global__ void sho_umma_colmax_kernel(const float2* __restrict__ in, long long L, int nb,
                                        unsigned* __restrict__ cmax, const int* active) {
@@ -586,10 +656,10 @@ __global__ void sho_umma_colmax_kernel(const float2* __restrict__ in, long long 
     if ((threadIdx.x & 31) == 0) atomicMax(cmax + c, __float_as_uint(m));
 }
 
-// B operand of coils c0 .. c0 + N0/2 - 1 in per-stage blocks: [sub][k / 8][row][k % 8] halves, sub =
-// cos part, sin part; rows 0 .. N0 - 1 the FP16 high parts of the N0 output columns (real parts of the
-// coils, then imaginary parts), rows N0 .. 2 N0 - 1 the low parts scaled by 2^11; inputs >= L and coils
-// >= nb are zero.
+// B operand of coils c0 .. c0 + N0/2 - 1 in per-stage blocks of 2 N0 rows x 128 bytes (the swizzled
+// layout of the kernel's shared memory): rows 0 .. N0 - 1 the FP16 high parts of the N0 output columns
+// (real parts of the coils, then imaginary parts), rows N0 .. 2 N0 - 1 the low parts scaled by 2^11;
+// per row the 32 inputs of the cos part, then of the sin part; inputs >= L and coils >= nb are zero.
 template <bool ADJ, int N0>
 __global__ void sho_umma_prep_kernel(const float2* __restrict__ in, long long L, long long Lpad, int nb, int c0,
                                      const unsigned* __restrict__ cmax, __half* __restrict__ b, const int* active) {
@@ -612,12 +682,13 @@ __global__ void sho_umma_prep_kernel(const float2* __restrict__ in, long long L,
     const long long q = i / KS;
     const int k = (int)(i - q * KS);
     __half* blk = b + q * (b_bytes(N0) / 2);
+    const int ch = k >> 3;   // 16-byte chunk of the cos part; the sin part's is 4 + ch
+    auto at = [&](int row, int c) { return blk + row * 64 + ((c ^ (row & 7)) << 3) + (k & 7); };
     auto put = [&](int sub, int n, float v) {
         const __half h = __float2half_rn(v);
         const __half l = __float2half_rn((v - __half2float(h)) * LO_SCALE);
-        __half* p = blk + (long long)sub * (2 * N0 * KS) + (long long)(k >> 3) * (2 * N0 * 8) + (k & 7);
-        p[n * 8] = h;
-        p[(N0 + n) * 8] = l;
+        *at(n, 4 * sub + ch) = h;
+        *at(N0 + n, 4 * sub + ch) = l;
     };
     put(0, cl, bc0);
     put(0, N0 / 2 + cl, bc1);
@@ -647,27 +718,16 @@ __global__ void sho_umma_reduce_kernel(const float* __restrict__ partial, int ns
 }
 
 // ------------------------------------------------------------------------ host --
-static PFN_cuTensorMapEncodeTiled_v12000 umma_encode_fn() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-    if (!fn) {
-        cudaDriverEntryPointQueryResult q;
-        void* f = nullptr;
-        MMR_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q));
-        MMR_REQUIRE(q == cudaDriverEntryPointSuccess && f, "cuTensorMapEncodeTiled unavailable");
-        fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
-    }
-    return fn;
-}
-
-// K split per row tile: the persistent CTAs get equal numbers of equal items, items as long as
-// the balance allows.
+// K split per row tile (in whole phase blocks): the persistent CTAs get equal numbers of equal
+// items, items as long as the balance allows.
 static int umma_nsplit(long long rtiles, long long Q, int nsm) {
+    const long long Qb = cdiv(Q, 4);
     int best = 1;
     double best_cost = 1e300;
-    for (int ns = 1; ns <= std::min<long long>(Q, 128); ++ns) {
+    for (int ns = 1; ns <= std::min<long long>(Qb, 128); ++ns) {
         const long long items = rtiles * ns;
         const long long per_cta = cdiv(items, std::min<long long>(items, nsm));
-        const double cost = (double)per_cta * ((double)cdiv(Q, ns) + 2.0);
+        const double cost = (double)per_cta * (4.0 * (double)cdiv(Qb, ns) + 2.0);
         if (cost < best_cost - 1e-9) {
             best_cost = cost;
             best = ns;
@@ -679,31 +739,27 @@ static int umma_nsplit(long long rtiles, long long Q, int nsm) {
 bool sho_umma_prepare(ShoUmma& u, const float* turn, long long V, long long M) {
     using namespace umma;
     u.ok = false;
-    // TMA: the table's row pitch (M floats) must be a multiple of 16 bytes, tile coordinates fit int
-    if (M % 4 != 0 || V > (1LL << 30) || M > (1LL << 30)) return false;
+    if (V > (1LL << 30) || M > (1LL << 30)) return false;   // tile coordinates fit int
     int major = 0, dev = 0;
     MMR_CUDA(cudaGetDevice(&dev));
     MMR_CUDA(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev));
     if (major != 10) return false;
-    const cuuint64_t dims[2] = {(cuuint64_t)M, (cuuint64_t)V};
-    const cuuint64_t strides[1] = {(cuuint64_t)M * 4};
-    const cuuint32_t estr[2] = {1, 1};
-    const cuuint32_t box_f[2] = {(cuuint32_t)BM, (cuuint32_t)KS};
-    const cuuint32_t box_a[2] = {(cuuint32_t)KS, (cuuint32_t)BM};
-    CUresult r = umma_encode_fn()(&u.map_fwd, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(turn), dims,
-                                  strides, box_f, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    MMR_REQUIRE(r == CUDA_SUCCESS, "cuTensorMapEncodeTiled (phase table, forward) failed (%d)", (int)r);
-    r = umma_encode_fn()(&u.map_adj, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(turn), dims, strides,
-                         box_a, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
-                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    MMR_REQUIRE(r == CUDA_SUCCESS, "cuTensorMapEncodeTiled (phase table, adjoint) failed (%d)", (int)r);
+    // the blocked copy of the table, when it fits in half of the free memory
+    const long long vblk = cdiv(V, BM), mblk = cdiv(M, BM);
+    const size_t tb_bytes = (size_t)vblk * (size_t)mblk * BM * BM * sizeof(float);
+    size_t fr = 0, tot = 0;
+    MMR_CUDA(cudaMemGetInfo(&fr, &tot));
+    if (tb_bytes > fr / 2) return false;
+    u.tblk.ensure(tb_bytes);
+    u.mblk = mblk;
+    sho_umma_block_kernel<<<(unsigned)(vblk * mblk), 256>>>(turn, V, M, mblk, u.tblk.as<float>());
+    check_launch("sho_umma_block");
     const int nsm = device_sm_count();
-    u.lpad = cdiv(std::max(V, M), KS) * KS;
+    u.lpad = cdiv(std::max(V, M), BM) * BM;   // inputs padded to whole phase blocks (4 stages)
     u.b.ensure((size_t)(u.lpad / KS) * b_bytes(64));
     for (int d = 0; d < 2; ++d) {
         const long long R = d ? V : M, L = d ? M : V;
-        u.nsplit[d] = umma_nsplit(cdiv(R, BM), cdiv(L, KS), nsm);
+        u.nsplit[d] = umma_nsplit(cdiv(R, BM), 4 * cdiv(L, BM), nsm);
     }
     u.partial.ensure((size_t)std::max(u.nsplit[0] * M, u.nsplit[1] * V) * 64 * sizeof(float));
     u.cmax.ensure((size_t)SHO_TC_MAX_COILS * sizeof(unsigned));
@@ -727,7 +783,7 @@ static void umma_group(ShoUmma& u, long long V, long long M, const float2* in, f
                        cudaStream_t st, const int* active) {
     using namespace umma;
     const long long R = ADJ ? V : M, L = ADJ ? M : V;
-    const long long Q = cdiv(L, KS);
+    const long long Q = 4 * cdiv(L, BM);   // stages, padded to whole phase blocks: every item has an even count
     const int nsplit = u.nsplit[ADJ ? 1 : 0];
     const long long nitems = cdiv(R, BM) * nsplit;
     const unsigned* cm = u.cmax.as<unsigned>();
@@ -736,9 +792,8 @@ static void umma_group(ShoUmma& u, long long V, long long M, const float2* in, f
                                                                                               c0, cm, b, active);
     check_launch("sho_umma_prep");
     const unsigned grid = (unsigned)std::min<long long>(nitems, device_sm_count());
-    sho_umma_kernel<ADJ, N0><<<grid, nthreads(N0), smem_bytes(N0), st>>>(ADJ ? u.map_adj : u.map_fwd, b,
-                                                                          u.partial.as<float>(), R, Q, nsplit, nitems,
-                                                                          u.err, active);
+    sho_umma_kernel<ADJ, N0><<<grid, nthreads(N0), smem_bytes(N0), st>>>(
+        u.tblk.as<float>(), V, M, u.mblk, b, u.partial.as<float>(), Q, nsplit, nitems, u.err, active);
     check_launch("sho_umma");
     // 1/sqrt(V) (sampHighOrder.m:387) and the 2^-11 of the A operand's fixed-point high parts
     const float scale = (float)(1.0 / std::sqrt((double)V) / 2048.0);

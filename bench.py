@@ -456,6 +456,26 @@ def highorder_measure(dev, reps=5, nit=30):
                              "rel_err_forward_vs_fp64_256_samples": rel1}}
 
 
+def highorder_profile_case(dev, apps=2):
+    """Profiling case for the high-order encoding kernels: the operator of highorder_measure
+    (128 x 128, 16384-sample spiral, 16 SH terms) applied `apps` times forward and adjoint to
+    16 coil images; prints one line."""
+    import matmri_gb300 as mm
+    from matmri_gb300 import synth
+    import torch
+    b0, t, spha, conc, grid = synth.highorder_inputs(128, 16384)
+    S = mm.sampHighOrder(b0, t, spha, conc, grid)
+    rng = np.random.default_rng(5)
+    x = (rng.standard_normal((128, 128, 16)) + 1j * rng.standard_normal((128, 128, 16))).astype(np.complex64)
+    xd = _dev_cm(x, dev)
+    yd = S * xd
+    for _ in range(apps):
+        yd = S * xd
+        S.H * yd
+    torch.cuda.synchronize(dev)
+    print("highorder profile case: %d forward + %d adjoint 16-coil applications" % (apps + 1, apps), flush=True)
+
+
 def finddel_measure(dev, cpu=True):
     """findDelAuto (delay between a field trajectory and the data): wall time of a whole estimation on
     the GPU at 64 x 64, 8 coils, 4096 samples, maxNit 15 (data simulated by the device encoding at a
@@ -676,9 +696,16 @@ def main():
                     help="fixed knobs coil_chunk,tile,coil_group,item,fft_lines,normal_mode (skips the autotuner)")
     ap.add_argument("--ncu", action="store_true",
                     help="profiling mode: one warm-up solve, then one solve; prints nothing else")
+    ap.add_argument("--ncu-highorder", action="store_true",
+                    help="profiling mode for the high-order encoding: 3 forward + 2 adjoint applications")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.ncu_highorder:
+        import torch
+        _, _, local = dist_env()
+        torch.cuda.set_device(local)
+        return highorder_profile_case(torch.device("cuda", local))
 
     import ctypes as C
     import torch

@@ -642,10 +642,12 @@ __global__ void sho_umma_block_kernel(const float* __restrict__ turn, long long 
     }
 }
 
-// Per-column max |re|, |im| of in[L, nb] as float bits (cmax zeroed by the caller).
+// Per-column max |re|, |im| of in[L, nb] as float bits (cmax zeroed by the caller): a block
+// reduction, one atomic per block and column.
 __global__ void sho_umma_colmax_kernel(const float2* __restrict__ in, long long L, int nb,
                                        unsigned* __restrict__ cmax, const int* active) {
     if (active && *active) return;
+    __shared__ float red[32];
     const int c = blockIdx.y;
     float m = 0.f;
     for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < L; i += (long long)gridDim.x * blockDim.x) {
@@ -653,7 +655,13 @@ __global__ void sho_umma_colmax_kernel(const float2* __restrict__ in, long long 
         m = fmaxf(m, fmaxf(fabsf(v.x), fabsf(v.y)));
     }
     for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
-    if ((threadIdx.x & 31) == 0) atomicMax(cmax + c, __float_as_uint(m));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = m;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        m = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : 0.f;
+        for (int o = 16; o; o >>= 1) m = fmaxf(m, __shfl_xor_sync(0xffffffffu, m, o));
+        if (threadIdx.x == 0) atomicMax(cmax + c, __float_as_uint(m));
+    }
 }
 
 // B operand of coils c0 .. c0 + N0/2 - 1 in per-stage blocks of 2 N0 rows x 128 bytes (the swizzled
@@ -697,24 +705,34 @@ __global__ void sho_umma_prep_kernel(const float2* __restrict__ in, long long L,
 }
 
 // out[row + R c] = scale * max|in_c| * (sum_sp partial[sp][row][cl] + i partial[sp][row][N0/2 + cl]),
-// summed over the splits in a fixed order (FP64).
+// summed over the splits in a fixed order (FP64).  A block takes 32 rows: it reads their partial rows
+// contiguously (N0 floats each) and writes each coil's 32 outputs contiguously, through a transposing
+// shared-memory tile.
 template <int N0>
-__global__ void sho_umma_reduce_kernel(const float* __restrict__ partial, int nsplit, long long R, int nb, int c0,
-                                       const unsigned* __restrict__ cmax, float scale, float2* __restrict__ out,
-                                       const int* active) {
+__global__ void __launch_bounds__(256) sho_umma_reduce_kernel(const float* __restrict__ partial, int nsplit, long long R,
+                                                               int nb, int c0, const unsigned* __restrict__ cmax,
+                                                               float scale, float2* __restrict__ out, const int* active) {
     if (active && *active) return;
-    const long long row = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-    const int cl = blockIdx.y;
-    const int c = c0 + cl;
-    if (row >= R || c >= nb) return;
-    double re = 0, im = 0;
-    for (int s = 0; s < nsplit; ++s) {
-        const float* p = partial + ((size_t)s * R + row) * N0;
-        re += p[cl];
-        im += p[N0 / 2 + cl];
+    constexpr int RB = 32;
+    __shared__ float tile[N0][RB + 1];
+    const long long row0 = (long long)blockIdx.x * RB;
+    for (int e = threadIdx.x; e < RB * N0; e += blockDim.x) {
+        const int i = e / N0, col = e - i * N0;    // consecutive threads: consecutive columns of a row
+        const long long row = row0 + i;
+        double acc = 0.0;
+        if (row < R)
+            for (int sp = 0; sp < nsplit; ++sp) acc += partial[((size_t)sp * R + row) * N0 + col];
+        tile[col][i] = (float)acc;
     }
-    const float f = scale * __uint_as_float(cmax[c]);
-    out[row + R * c] = make_float2((float)re * f, (float)im * f);
+    __syncthreads();
+    for (int e = threadIdx.x; e < RB * (N0 / 2); e += blockDim.x) {
+        const int cl = e / RB, i = e - cl * RB;    // consecutive threads: consecutive rows of a coil
+        const int c = c0 + cl;
+        const long long row = row0 + i;
+        if (row >= R || c >= nb) continue;
+        const float f = scale * __uint_as_float(cmax[c]);
+        out[row + R * c] = make_float2(tile[cl][i] * f, tile[N0 / 2 + cl][i] * f);
+    }
 }
 
 // ------------------------------------------------------------------------ host --
@@ -797,7 +815,7 @@ static void umma_group(ShoUmma& u, long long V, long long M, const float2* in, f
     check_launch("sho_umma");
     // 1/sqrt(V) (sampHighOrder.m:387) and the 2^-11 of the A operand's fixed-point high parts
     const float scale = (float)(1.0 / std::sqrt((double)V) / 2048.0);
-    sho_umma_reduce_kernel<N0><<<dim3((unsigned)cdiv(R, 256), N0 / 2), 256, 0, st>>>(
+    sho_umma_reduce_kernel<N0><<<(unsigned)cdiv(R, 32), 256, 0, st>>>(
         u.partial.as<float>(), nsplit, R, (int)nb, c0, cm, scale, out, active);
     check_launch("sho_umma_reduce");
 }
@@ -809,7 +827,7 @@ static void umma_apply(ShoUmma& u, long long V, long long M, const float2* in, f
     MMR_REQUIRE(nb >= 1 && nb <= SHO_TC_MAX_COILS, "tensor-core encoding handles 1..%lld columns", SHO_TC_MAX_COILS);
     const long long L = ADJ ? M : V;
     MMR_CUDA(cudaMemsetAsync(u.cmax.p, 0, (size_t)nb * sizeof(unsigned), st));
-    sho_umma_colmax_kernel<<<dim3((unsigned)std::min<long long>(cdiv(L, 256), 256), (unsigned)nb), 256, 0, st>>>(
+    sho_umma_colmax_kernel<<<dim3((unsigned)std::min<long long>(cdiv(L, 1024), 64), (unsigned)nb), 256, 0, st>>>(
         in, L, (int)nb, u.cmax.as<unsigned>(), active);
     check_launch("sho_umma_colmax");
     if (nb <= 8) {

@@ -21,31 +21,37 @@
 // sets in FP32 registers and the split-K partials are summed in FP64 in a
 // fixed order by a second kernel.
 //
-// One persistent CTA per SM walks (row tile, K split) work items; warp roles
-// (16 producer warps for up to 16 coils per pass, 8 for 32):
+// One persistent CTA per SM walks (row tile, K split) work items (whole 128-input
+// phase blocks, so every item has an even number of 32-input stages, taken in
+// chunks of two); warp roles (16 producer warps for up to 16 coils per pass, 8
+// for 32):
 //   producers   per stage (32 inputs x 128 rows) load their phases straight
-//               from global memory one stage ahead, into registers (thread 0
-//               also issues a bulk L2 prefetch of the phase tile sixteen stages
-//               ahead), evaluate sincos on the SFU, split to FP16 hi/lo and
-//               store the A operand in the no-swizzle K-major UMMA layout into
-//               a 6-deep ring (5 for 32-coil groups);
-//   B loader    one bulk copy per stage of the pre-split coil data into a
-//               4-deep ring that the MMA thread releases;
-//   MMA warp    one thread issues tcgen05.mma (kind::f16, M 128, K 16),
-//               commits stage completion to the operand rings' mbarriers and
-//               chunk completion to its own, and after seeing a chunk complete
-//               hands its accumulation set to the epilogue; the warp owns the
-//               TMEM allocation (all 512 columns);
-//   4 epilogue warps: every two stages (64 inputs) the MMA warp moves on to the
-//               next accumulation set of a TMEM ring, and the epilogue warps
-//               (each its 32-lane quarter) read the finished set with
-//               tcgen05.ld and add it to FP32 register totals, which they store
-//               as the item's partial sums at its end.
-// The A ring is as deep as shared memory allows because the tensor pipe idles
-// whenever the producers cannot refill a slot while the MMAs of the others
-// run; the phase table needs no shared-memory staging of its own.
-// Generic stores into an A slot that MMAs read through the async proxy follow
-// a fence.proxy.async after the slot's release; without it, adjoint rows came
+//               from global memory two stages ahead into registers (thread 0
+//               also issues a bulk L2 prefetch of the phase block quarter
+//               sixteen stages ahead), evaluate sincos on the SFU, split to
+//               FP16 hi/lo and store the A operand, 128-byte swizzled, into a
+//               6-deep ring (4 for 32-coil groups); once per chunk they hand
+//               the previous chunk to the MMA thread (a proxy fence, then one
+//               arrival per warp) and wait for the chunk that last used their
+//               slots;
+//   B loader    one bulk copy per chunk of the pre-split coil data into a
+//               2-chunk ring, completing on the chunk slot's mbarrier;
+//   MMA warp    one thread: per chunk it probes three barriers (accumulation
+//               set free, A stored, B landed) with back-to-back test_waits,
+//               issues 16 tcgen05.mma (kind::f16, M 128, K 16) behind one
+//               tcgen05 fence, and commits twice: the chunk's A and B slots,
+//               and its accumulation set to the epilogue.  An mbarrier wait or
+//               a tcgen05 fence costs this thread a few hundred cycles, about
+//               the issue time of six MMAs, so there is one of each per 16
+//               MMAs.  The warp owns the TMEM allocation (all 512 columns);
+//   4 epilogue warps: per chunk (64 inputs) the MMA warp moves on to the next
+//               accumulation set of a TMEM ring, and the epilogue warps (each
+//               its 32-lane quarter) wait for the set's commit, read it with
+//               tcgen05.ld and add it to FP32 register totals, which they
+//               store as the item's partial sums at its end.
+// The A ring is as deep as shared memory allows: the producers run up to three
+// chunks ahead of the tensor pipe.  Generic stores into an A slot are followed
+// by a fence.proxy.async before the hand-off; without it, adjoint rows came
 // out wrong on a GB300.
 // The B operand stacks hi and lo rows, so per 16 inputs and per cos / sin part
 // two MMAs cover the three products: A_hi x [B_hi; B_lo] (N = 2 N0: main and

@@ -4,11 +4,12 @@
 // imMask (Vm of them),
 //   S   = exp(1i * kbase(mask, :)).' / sqrt(Vm)                [M x Vm]
 //   AtA = sum_c conj(r_c) r_c.' .* (S' * S)                    [Vm x Vm]
-// with r_c the coil-c sensitivities on the mask.  Here the encoding matrix
-// E = exp(1i kbase).' is written once from the plan's phase table (sincospi of
-// the FP32 turns, sho.cu), the Gram S'S is one complex GEMM in cuBLAS with the
-// FP32 BF16x9 emulation (tensor cores at FP32 accuracy; a plain library GEMM),
-// and the coil weighting runs as a tiled in-place epilogue.  The direct solve
+// with r_c the coil-c sensitivities on the mask.  Here the Gram S'S runs on the
+// repository's own tcgen05 kernel (gram_umma.cu): the encoding rows are written
+// once as FP16 hi / lo parts of cos and sin (sincospi of the plan's FP32 turns,
+// sho.cu) and contracted with FP32 accumulation in TMEM.  On a device without
+// tcgen05 the Gram is one complex GEMM in cuBLAS with the FP32 BF16x9 emulation
+// instead.  The coil weighting runs as a tiled in-place epilogue.  The direct solve
 // of the demo (demos/demo_denseMat.m:98-106: lam2 added to the diagonal, then
 // AtA \ Aty) factors a copy with cuSOLVER: Cholesky, and LU when the shifted
 // matrix is not numerically positive definite (MATLAB's backslash makes the
@@ -101,16 +102,23 @@ void dense_normal(ShoPlan& S, const RcvrPlan* R, const long long* vox_h, long lo
     DevBuf d_vox, d_E;
     std::vector<long long> vh(vox_h, vox_h + nvox);
     d_vox.upload(vh);
-    d_E.ensure((size_t)M * nvox * sizeof(float2));
-    float2* E = d_E.as<float2>();
-    sho_encoding_matrix(S, d_vox.as<long long>(), nvox, E, st);
-    cublasHandle_t h = blas_handle();
-    MMR_CUBLAS(cublasSetStream(h, st));
-    const cuComplex alpha = make_cuComplex((float)(1.0 / (double)nvox), 0.f), beta = make_cuComplex(0.f, 0.f);
     // S'S with S = E / sqrt(nvox): (1/nvox) E^H E     (mrSampFuncMat.m:37-38)
-    MMR_CUBLAS(cublasCgemm(h, CUBLAS_OP_C, CUBLAS_OP_N, (int)nvox, (int)nvox, (int)M, &alpha,
-                           reinterpret_cast<const cuComplex*>(E), (int)M, reinterpret_cast<const cuComplex*>(E),
-                           (int)M, &beta, reinterpret_cast<cuComplex*>(AtA), (int)nvox));
+    if (gram_umma_supported()) {
+        const long long rows = cdiv(nvox, 128) * 128, kpad = cdiv(M, 128) * 128;
+        d_E.ensure((size_t)4 * rows * kpad * sizeof(__half));
+        sho_gram_operands(S, d_vox.as<long long>(), nvox, rows, kpad, d_E.as<__half>(), st);
+        MMR_REQUIRE(gram_umma(d_E.as<__half>(), nvox, rows, kpad, AtA, st), "tcgen05 Gram unavailable");
+    } else {
+        d_E.ensure((size_t)M * nvox * sizeof(float2));
+        float2* E = d_E.as<float2>();
+        sho_encoding_matrix(S, d_vox.as<long long>(), nvox, E, st);
+        cublasHandle_t h = blas_handle();
+        MMR_CUBLAS(cublasSetStream(h, st));
+        const cuComplex alpha = make_cuComplex((float)(1.0 / (double)nvox), 0.f), beta = make_cuComplex(0.f, 0.f);
+        MMR_CUBLAS(cublasCgemm(h, CUBLAS_OP_C, CUBLAS_OP_N, (int)nvox, (int)nvox, (int)M, &alpha,
+                               reinterpret_cast<const cuComplex*>(E), (int)M, reinterpret_cast<const cuComplex*>(E),
+                               (int)M, &beta, reinterpret_cast<cuComplex*>(AtA), (int)nvox));
+    }
     if (R) {
         dim3 grid((unsigned)cdiv(nvox, DT), (unsigned)cdiv(nvox, DT));
         coil_hadamard_kernel<<<grid, DT * 8, 0, st>>>(AtA, nvox, R->d_maps.as<float2>(), V, (int)R->C,

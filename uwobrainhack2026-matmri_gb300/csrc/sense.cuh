@@ -1,6 +1,8 @@
 // @rcvrOp, @sampHighOrder handle types and the mrSampFunc composition.
 #pragma once
 
+#include <cuda_fp16.h>
+
 #include "nufft.cuh"
 
 namespace mmr {
@@ -22,6 +24,14 @@ long long sho_nvox(const ShoPlan& s);
 long long sho_nsamp(const ShoPlan& s);
 // E [M, nvox] complex64, E[m + M j] = exp(i kbase[vox[j], m]) (vox: device indices).
 void sho_encoding_matrix(ShoPlan& s, const long long* vox, long long nvox, float2* E, cudaStream_t st);
+// The Gram operands [4][rows][kpad] FP16 (cos hi, cos lo, sin hi, sin lo; rows >= nvox, kpad >= M,
+// zero-padded) of the mask voxels' encoding rows.
+void sho_gram_operands(ShoPlan& s, const long long* vox, long long nvox, long long rows, long long kpad, __half* op,
+                       cudaStream_t st);
+// (1 / n) E^H E for the Gram operands above on the tcgen05 tensor cores, written to AtA [n x n]
+// column-major (both triangles); false when the device has no tcgen05.
+bool gram_umma(const __half* op, long long n, long long rows, long long kpad, float2* AtA, cudaStream_t st);
+bool gram_umma_supported();
 
 void rcvr_forward(const RcvrPlan& r, const float2* x, float2* y, cudaStream_t st, const int* active);
 void rcvr_adjoint(const RcvrPlan& r, const float2* y, float2* x, cudaStream_t st, const int* active);

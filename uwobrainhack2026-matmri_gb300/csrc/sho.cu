@@ -364,6 +364,43 @@ void sho_encoding_matrix(ShoPlan& s, const long long* vox, long long nvox, float
     check_launch("sho_emat");
 }
 
+// Operands of the dense Gram on the tensor cores: for mask voxel r (row) and sample k,
+// op[p][r][k] (FP16) with p = cos hi, cos lo, sin hi, sin lo of exp(i kbase[vox[r], k]): hi =
+// round(2^11 v), exact in FP16, lo = 2^11 v - hi.  Rows past nvox and samples past M are zero.
+__global__ void sho_gram_operands_kernel(const float* __restrict__ turn, const double* __restrict__ B,
+                                         const double* __restrict__ P, int K, long long V, long long M,
+                                         const long long* __restrict__ vox, long long nvox, long long rows,
+                                         long long kpad, __half* __restrict__ op) {
+    const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= rows * kpad) return;
+    const long long r = i / kpad, k = i - r * kpad;
+    float ch = 0.f, cl = 0.f, sh = 0.f, sl = 0.f;
+    if (r < nvox && k < M) {
+        const long long v = vox[r];
+        const float t = turn ? turn[v * M + k] : phase_turn(sho_phase(B, P, K, V, M, v, k));
+        float sn, cs;
+        sincospif(2.f * t, &sn, &cs);
+        ch = rintf(cs * 2048.f);
+        cl = fmaf(cs, 2048.f, -ch);
+        sh = rintf(sn * 2048.f);
+        sl = fmaf(sn, 2048.f, -sh);
+    }
+    const size_t plane = (size_t)rows * kpad;
+    op[i] = __float2half_rn(ch);
+    op[i + plane] = __float2half_rn(cl);
+    op[i + 2 * plane] = __float2half_rn(sh);
+    op[i + 3 * plane] = __float2half_rn(sl);
+}
+
+void sho_gram_operands(ShoPlan& s, const long long* vox, long long nvox, long long rows, long long kpad, __half* op,
+                       cudaStream_t st) {
+    MMR_REQUIRE(!s.base && !s.interp, "the dense encoding needs a direct sampHighOrder plan");
+    sho_gram_operands_kernel<<<(unsigned)cdiv(rows * kpad, 256), 256, 0, st>>>(
+        s.table ? s.d_turn.as<float>() : nullptr, s.d_B.as<double>(), s.d_P.as<double>(), s.K, s.V, s.M, vox, nvox,
+        rows, kpad, op);
+    check_launch("sho_gram_operands");
+}
+
 static void sho_build(ShoPlan& s, const mmr_sho_desc& d) {
     MMR_REQUIRE(d.ndim >= 1 && d.ndim <= 3, "ndim must be 1..3");
     MMR_REQUIRE(d.nsamp >= 1 && d.t && d.spha && d.gx && d.gy && d.gz, "missing sampHighOrder input");

@@ -60,6 +60,14 @@ MMR_API int  mmr_device_info(int* sm_count, int* smem_optin_bytes, int* cc_major
 /* Kernels this library has launched in the process (eager launches plus the
  * kernel nodes of every replayed CUDA graph). */
 MMR_API int  mmr_kernel_launches(uint64_t* count);
+/* Reports a bounded device wait that ran out since the last check, for callers that pass
+ * device pointers (entry points given host buffers check it themselves before returning):
+ * synchronises `stream`, returns MMR_ERR_TIMEOUT and clears the flag if it was set, else
+ * MMR_OK.  No reference counterpart (MATLAB has no asynchronous device calls). */
+MMR_API int  mmr_check_device_error(void* stream);
+/* Test hook: poll limit of the gridding kernels' bounded TMA waits (default 4194304; 0 makes
+ * every wait run out, after which the kernel still lets its copy land and returns). */
+MMR_API int  mmr_debug_set_wait_polls(int32_t polls);
 
 /* ---- @nufftOp ------------------------------------------------------------
  * Replaces nufftOp(imN, kloc, dcf, useGPU, os, kwidth)

@@ -37,12 +37,20 @@
 namespace mmr {
 
 __device__ int g_dev_error = 0;
+// Poll limit of the gridding kernels' bounded TMA waits; a test lowers it to make a wait run out.
+constexpr int kDefaultWaitPolls = 1 << 22;
+__device__ int g_wait_polls = kDefaultWaitPolls;
 
 // Device address of the error word, for kernels of other translation units that take it as an argument.
 int* device_error_ptr() {
     int* p = nullptr;
     MMR_CUDA(cudaGetSymbolAddress((void**)&p, g_dev_error));
     return p;
+}
+
+void set_wait_polls(int polls) {
+    const int v = polls > 0 ? polls : 0;
+    MMR_CUDA(cudaMemcpyToSymbol(g_wait_polls, &v, sizeof(int)));
 }
 
 int device_error_word(cudaStream_t st) {
@@ -389,10 +397,8 @@ __device__ __forceinline__ uint32_t smem_u32(const void* p) {
     return (uint32_t)__cvta_generic_to_shared(p);
 }
 
-// Bounded mbarrier wait: returns false (and flags the device error word) on timeout.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
-    const uint32_t a = smem_u32(bar);
-    for (int it = 0; it < (1 << 22); ++it) {
+__device__ __forceinline__ bool mbar_poll(uint32_t a, uint32_t phase, int polls) {
+    for (int it = 0; it < polls; ++it) {
         uint32_t done;
         asm volatile(
             "{\n\t.reg .pred p;\n\t"
@@ -403,7 +409,18 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
             : "memory");
         if (done) return true;
     }
+    return false;
+}
+
+// Bounded mbarrier wait for a TMA copy: returns false (and flags the device error word) when
+// g_wait_polls polls run out.  Before it returns false it still waits (bounded, with the default
+// limit) for the copy to land, so that the CTA never leaves with a copy into its shared memory in
+// flight.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t phase) {
+    const uint32_t a = smem_u32(bar);
+    if (mbar_poll(a, phase, g_wait_polls)) return true;
     atomicExch(&g_dev_error, 1);
+    mbar_poll(a, phase, kDefaultWaitPolls);
     return false;
 }
 

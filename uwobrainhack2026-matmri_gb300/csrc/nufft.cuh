@@ -129,6 +129,8 @@ void nufft_grid_normal_stencil(NufftPlan& p, const float2* gin, float2* gout, lo
 
 // Device error word set by bounded waits that ran out (0 = none).
 int device_error_word(cudaStream_t st);
+// Sets the poll limit of the gridding kernels' bounded TMA waits (test hook; 0 makes every wait run out).
+void set_wait_polls(int polls);
 int* device_error_ptr();
 
 }  // namespace mmr

@@ -322,6 +322,19 @@ extern "C" int mmr_nufft_apply(mmr_nufft* plan, int adjoint, const void* in, voi
     });
 }
 
+extern "C" int mmr_check_device_error(void* stream) {
+    return guarded([&] {
+        if (device_error_word(as_stream(stream))) MMR_THROW(MMR_ERR_TIMEOUT, "a bounded device wait ran out");
+    });
+}
+
+extern "C" int mmr_debug_set_wait_polls(int32_t polls) {
+    return guarded([&] {
+        MMR_REQUIRE(polls >= 0, "polls must be >= 0");
+        set_wait_polls(polls);
+    });
+}
+
 extern "C" int mmr_nufft_prep_toep(mmr_nufft* plan, double tos, int32_t kwidth) {
     return guarded([&] {
         MMR_REQUIRE(plan, "NULL plan");

@@ -105,6 +105,8 @@ SIGNATURES = {
     "mmr_abi_version": (C.c_int, []),
     "mmr_last_error": (C.c_int, [C.c_char_p, C.c_size_t]),
     "mmr_device_info": (C.c_int, [C.POINTER(C.c_int)] * 4),
+    "mmr_check_device_error": (C.c_int, [C.c_void_p]),
+    "mmr_debug_set_wait_polls": (C.c_int, [C.c_int32]),
     "mmr_kernel_launches": (C.c_int, [C.POINTER(C.c_uint64)]),
     "mmr_sense_profile_normal": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.POINTER(C.c_double),
                                            C.POINTER(C.c_int32), C.c_void_p]),
@@ -189,6 +191,14 @@ def check(code: int):
         buf = C.create_string_buffer(1024)
         load().mmr_last_error(buf, 1024)
         raise MatmriError(code, buf.value.decode(errors="replace"))
+
+
+def check_device_error(stream=None):
+    """Raises MatmriError (TIMEOUT) when a bounded device wait ran out since the last check, and
+    clears the flag.  For callers that pass device arrays: calls given host arrays check it
+    themselves before returning.  `stream`: a cudaStream_t handle (int) or None for the default
+    stream; it is synchronised."""
+    check(load().mmr_check_device_error(C.c_void_p(stream or 0)))
 
 
 def dptr(a: np.ndarray):

@@ -26,7 +26,7 @@
 // chunks of two); warp roles (16 producer warps for up to 16 coils per pass, 8
 // for 32):
 //   producers   per stage (32 inputs x 128 rows) load their phases straight
-//               from global memory two stages ahead into registers (thread 0
+//               from global memory one stage ahead into registers (thread 0
 //               also issues a bulk L2 prefetch of the phase block quarter
 //               sixteen stages ahead), evaluate sincos on the SFU, split to
 //               FP16 hi/lo and store the A operand, 128-byte swizzled, into a
@@ -82,7 +82,7 @@ constexpr int PF = 16;                       // L2 prefetch distance of the phas
 constexpr int MAX_SA = 6;
 constexpr int QUARTER_BYTES = BM * KS * 4;   // one stage's phases: a quarter of a 128 x 128 block (16 KB)
 static_assert(BM == 4 * KS, "a phase block holds four stages along the input dimension");
-constexpr int LA = 2;                        // stages of phases each producer thread keeps in flight
+constexpr int LA = 1;                        // stages of phases each producer thread keeps in flight
 // Operands in the 128-byte-swizzled K-major layout: rows of 128 bytes, 16-byte chunk c of row r at
 // chunk position c ^ (r & 7), 8-row groups 1 KB apart.  An A stage is two 128-row regions, the
 // cos region holding [hi (32 inputs, 64 B) | lo (64 B)] per row and the sin region the same; a B

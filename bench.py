@@ -481,6 +481,23 @@ def highorder_profile_case(dev, apps=2):
     print("highorder profile case: %d forward + %d adjoint 16-coil applications" % (apps + 1, apps), flush=True)
 
 
+def dense_profile_case(dev, n_img=64, M=4096, C=8):
+    """Profiling case for the dense Gram kernel: mrSampFuncMat at n_img x n_img voxels, M samples,
+    C coils, full mask, built twice; prints one line."""
+    import torch
+    import matmri_gb300 as mm
+    from matmri_gb300 import synth
+    b0, t, spha, conc, grid = synth.highorder_inputs(n_img, M)
+    maps = synth.coil_maps(n_img, C, 3001)
+    rng = np.random.default_rng(9)
+    y = (rng.standard_normal((M, C)) + 1j * rng.standard_normal((M, C))).astype(np.complex64)
+    for _ in range(2):
+        AtA, _ = mm.mrSampFuncMat(y, maps, b0, t, spha, conc, grid)
+    torch.cuda.synchronize(dev)
+    print("dense profile case: %d x %d Gram over %d samples, built twice" % (AtA.shape[0], AtA.shape[1], M),
+          flush=True)
+
+
 def finddel_measure(dev, cpu=True):
     """findDelAuto (delay between a field trajectory and the data): wall time of a whole estimation on
     the GPU at 64 x 64, 8 coils, 4096 samples, maxNit 15 (data simulated by the device encoding at a
@@ -703,14 +720,17 @@ def main():
                     help="profiling mode: one warm-up solve, then one solve; prints nothing else")
     ap.add_argument("--ncu-highorder", action="store_true",
                     help="profiling mode for the high-order encoding: 3 forward + 2 adjoint applications")
+    ap.add_argument("--ncu-dense", action="store_true",
+                    help="profiling mode for the dense Gram: a 4096^2 mrSampFuncMat built twice")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
-    if args.ncu_highorder:
+    if args.ncu_highorder or args.ncu_dense:
         import torch
         _, _, local = dist_env()
         torch.cuda.set_device(local)
-        return highorder_profile_case(torch.device("cuda", local))
+        dev = torch.device("cuda", local)
+        return highorder_profile_case(dev) if args.ncu_highorder else dense_profile_case(dev)
 
     import ctypes as C
     import torch

@@ -683,5 +683,12 @@ void mexFunction(int nlhs, mxArray* plhs[], int nrhs, const mxArray* prhs[]) {
         if (nlhs > 1) plhs[1] = mxCreateDoubleScalar(method);
         return;
     }
+    /* --------------------------------------------------------------- library */
+    if (!strcmp(cmd, "check_device_error")) {
+        /* () raises matmri:gb300:e4 if a bounded device wait ran out during a call given gpuArray
+           data (calls given host arrays report it themselves); clears the flag */
+        check(mmr_check_device_error(NULL));
+        return;
+    }
     mexErrMsgIdAndTxt("matmri:gb300:arg", "unknown command %s", cmd);
 }

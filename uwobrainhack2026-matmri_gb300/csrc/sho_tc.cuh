@@ -19,15 +19,16 @@ struct ShoTcScratch {
 
 void sho_tc_alloc(ShoTcScratch& s, long long V, long long M);
 
-// tcgen05 path (sho_umma.cu): TMA tensor maps of the phase table and the device scratch of one plan.
+// tcgen05 path (sho_umma.cu): the blocked radians copy of the phase table and the device scratch of
+// one plan.
 struct ShoUmma {
     bool ok = false;
-    DevBuf tblk;            // the phase table in 128 x 128 blocks [V / 128][M / 128][128][128]
+    DevBuf tblk;            // the phase table as radians in 128 x 128 blocks [V / 128][M / 128][128][128]
     long long mblk = 0;     // blocks along M
-    DevBuf b;               // B operand per stage (largest coil group), FP16 hi / lo
+    DevBuf b;               // B operand per stage (largest coil group), FP16 hi / lo, swizzled
     DevBuf partial;         // split-K partial sums [nsplit][rows][2 coils]
     DevBuf cmax;            // per-column max |re|, |im|
-    long long lpad = 0;
+    long long lpad = 0;     // inputs padded to whole phase blocks (128)
     int nsplit[2] = {1, 1};   // forward, adjoint
     int* err = nullptr;       // device error word
 };

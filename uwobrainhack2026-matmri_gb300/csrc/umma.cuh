@@ -10,7 +10,7 @@ namespace mmr {
 namespace umma {
 
 // mbarrier waits: each try_wait may suspend the thread for up to SUSPEND_NS (it resumes as soon as
-// the phase completes), so that waiting warps take no issue slots from the producers; at most
+// the phase completes), so that waiting warps take few issue slots from the working ones; at most
 // WAIT_POLLS polls (about a second) before a wait counts as timed out
 constexpr uint32_t SUSPEND_NS = 500;
 constexpr uint32_t WAIT_POLLS = 1u << 21;
